@@ -1,0 +1,413 @@
+"""Benchmark of the GB300 Euler step (Gcell-updates/s), one JSON line.
+
+Workload (the reference's per-operator benchmark configuration, scaled to one
+fused step): a 512^3-interior grid (514^3 with ghosts, following
+benchmarks/benchmark_godunov.cpp:18) holding a seeded random state -- rho and
+p log-uniform on [0.1, 10], each velocity component N(0, 1), gamma = 1.4,
+dx = 1/512, CFL 0.4 -- advanced by the fused step (time_step -> godunov ->
+cons_to_prim of simulations/euler_simulation.cpp:57-67 in one pass).  A step
+updates 512^3 interior cells.  Inputs are 5.4 GB per bundle, far larger than
+L2, so no flush is needed between steps.
+
+Reported:
+  value      device-resident throughput (state already in HBM)
+  e2e        the same step through the C ABI from host buffers: host->device
+             prim, step, device->host prim, every step
+  roofline   the fused kernel against the FP64 pipe: algorithmic FLOPs per
+             interior cell x cells / CUDA-event kernel time, over the FP64 FMA
+             rate measured on this GPU in the same run
+  operators  each reference operator alone at 514^3 (prim_to_cons,
+             cons_to_prim, time_step, godunov), CUDA-event timed
+  cpu_baseline  the CPU oracle (C restatement of the reference operators,
+             OpenMP on all host cores) on a bounded slab of the same workload
+
+`--impl reference` times the reference's CPU implementation instead (the
+oracle port; the reference's own sources are not present where this runs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "benchmark-euler-kernels_gb300")
+for _p in (ROOT, PKG_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Gcell-updates/s per step, plain FP64 vs FP32-compensated at stated L1 error"
+UNIT = "Gcell-updates/s"
+GAMMA = 1.4
+CFL = 0.4
+
+# Algorithmic FP64 flops per interior cell of one fused step: each face solved
+# once (3 faces per cell), the conservative update, cons_to_prim of the new
+# state and the next step's wavespeed.  +,-,*,/,sqrt count 1, min/max/abs/
+# select 0.  Counted by instantiating the reference's own hllc/godunov/
+# cons_to_prim/time_step arithmetic with a counting scalar (oracle/count_flops.cpp).
+FLOPS_PER_CELL_DEFAULT = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=512, help="interior cells per axis")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ops", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def flops_per_cell():
+    path = os.path.join(ROOT, "oracle", "flops_per_cell.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------- CPU
+def cpu_baseline(n: int, seconds: float):
+    """The oracle (C restatement of the reference operators, OpenMP over all
+    host cores) on a slab of the workload: n x n x kz interior cells, with kz
+    sized so the run takes about `seconds`."""
+    import numpy as np
+
+    import oracle as O
+
+    O.build(ref=False)
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    kz = 4
+    dx = (1.0 / n,) * 3
+    prim = O.random_prim(n + 2, n + 2, kz + 2, seed=0)
+    cons = O.prim_to_cons(prim, GAMMA)
+    t0 = time.perf_counter()
+    O.simulate(prim, cons, GAMMA, dx, CFL, 1)
+    one = time.perf_counter() - t0
+    steps = max(1, int(seconds / max(one, 1e-6)))
+    t0 = time.perf_counter()
+    O.simulate(prim, cons, GAMMA, dx, CFL, steps)
+    el = time.perf_counter() - t0
+    cells = n * n * kz * steps
+    return {
+        "value": cells / el / 1e9,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{steps} steps of the reference loop (time_step, godunov, cons_to_prim) on a "
+                  f"{n}x{n}x{kz}-interior slab of the same random state, {el:.1f} s",
+        "_np": np.__version__,
+    }
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    res = cpu_baseline(args.n, args.cpu_seconds)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"fused Euler step, {args.n}^3 interior, seeded random state", "n": args.n,
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {k: v for k, v in res.items() if not k.startswith("_")},
+        "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference arm: the reference's CPU implementation of the path, as the oracle port (the "
+                "reference sources are not present on the GPU host); OpenMP over all host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------- GPU
+def random_prim_device(torch, n0, n1, n2, seed=0):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    prim = torch.empty((5, n2, n1, n0), dtype=torch.float64, device="cuda")
+    lo, hi = torch.log(torch.tensor(0.1)).item(), torch.log(torch.tensor(10.0)).item()
+    for f in (0, 1):
+        prim[f].uniform_(lo, hi, generator=g)
+        prim[f].exp_()
+    for f in (2, 3, 4):
+        prim[f].normal_(0.0, 1.0, generator=g)
+    return prim
+
+
+def time_ops(torch, E, prim, n_int):
+    """Each reference operator alone, one call after warm-up (CUDA events)."""
+    n0 = n_int + 2
+    dx = (1.0 / n_int,) * 3
+    cons = E.prim_to_cons(prim, GAMMA)
+    prim2 = torch.empty_like(prim)
+    dt = E.time_step(prim, GAMMA, dx)
+    cells = n0 ** 3
+    interior = n_int ** 3
+    out = {}
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = None
+        for _ in range(reps):
+            s.record()
+            fn()
+            e.record()
+            e.synchronize()
+            ms = s.elapsed_time(e)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    # bytes: the reference's own counters (benchmarks/benchmark_*.cpp:37-52)
+    ms = timed(lambda: E.prim_to_cons(prim, GAMMA, out=cons))
+    out["prim_to_cons"] = {"ms": ms, "gcells_s": cells / ms / 1e6, "gb_s": 80 * cells / ms / 1e6}
+    ms = timed(lambda: E.cons_to_prim(cons, GAMMA, out=prim2))
+    out["cons_to_prim"] = {"ms": ms, "gcells_s": cells / ms / 1e6, "gb_s": 80 * cells / ms / 1e6}
+    ms = timed(lambda: E.time_step(prim, GAMMA, dx, out=dt))
+    out["time_step"] = {"ms": ms, "gcells_s": cells / ms / 1e6, "gb_s": 40 * cells / ms / 1e6}
+    ms = timed(lambda: E.godunov(prim, cons, GAMMA, dx, 1e-9))
+    out["godunov"] = {"ms": ms, "gcells_s": cells / ms / 1e6, "gb_s": 120 * cells / ms / 1e6,
+                      "interior_gcells_s": interior / ms / 1e6}
+    del cons, prim2
+    return out
+
+
+def run_ours(args):
+    import torch
+
+    import euler_gb300 as E
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    E.build()
+    E.load()
+    n = args.n
+    n0 = n + 2
+    dx = (1.0 / n,) * 3
+    interior = n ** 3
+    # a dedicated stream: the simulation captures its step loop into a CUDA
+    # graph (not possible on the legacy default stream) and the timing events
+    # are recorded on the same stream
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    # replicas: every rank advances its own grid, no data-path collective
+    prim = random_prim_device(torch, n0, n0, n0, seed=rank)
+    sim = E.Simulation(n0, n0, n0, GAMMA, dx, CFL, stream=stream)
+    sim.set_prim(prim)
+    del prim
+    torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        sim.advance(1)
+    torch.cuda.synchronize()
+    # per-launch device times of one step (the fused kernel dominates)
+    prof = [sim.profile_step() for _ in range(3)]
+    flux_ms = min(p[1] for p in prof)
+    step_ms_launches = min(sum(p) for p in prof)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    sim.advance(args.steps)
+    e.record(stream)
+    e.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ms = s.elapsed_time(e)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+    ms_per_step = ms / args.steps
+    value = world * interior * args.steps / (ms * 1e-3) / 1e9
+    status = sim.status()
+    t_sim, next_dt, nsteps = sim.time()
+    launches = args.steps * sim.launches_per_step()
+
+    # roofline of the fused kernel on the FP64 pipe
+    fpc = flops_per_cell()
+    peak = E.fma_rate("f64")
+    roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak / 1e12,
+            "peak_source": "measured in this run: FP64 FMA probe (eulr_probe_fma_rate), FMA = 2 FLOP",
+            "kernel": "flux_tile_kernel<double, step>", "kernel_ms": flux_ms,
+            "step_ms_sum_of_launches": step_ms_launches, "traffic": None}
+    if fpc:
+        fl = fpc["fused_step_fp64"] * interior
+        roof["achieved"] = fl / (flux_ms * 1e-3) / 1e12
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        roof["flops_per_cell"] = fpc["fused_step_fp64"]
+    else:
+        roof["achieved"] = None
+        roof["frac"] = None
+    # the same kernel against HBM (algorithmic 80 B per interior cell:
+    # cons read + cons written)
+    hbm_peak = None
+    mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(mp):
+        with open(mp) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+    hbm = {"algorithmic_bytes_per_cell": 80, "achieved_gbs": 80 * interior / (flux_ms * 1e-3) / 1e9,
+           "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json (measured)" if hbm_peak else None}
+    if hbm_peak:
+        hbm["frac"] = hbm["achieved_gbs"] / hbm_peak
+    roof["hbm"] = hbm
+
+    ops = None
+    if not args.no_ops and rank == 0:
+        prim = random_prim_device(torch, n0, n0, n0, seed=1)
+        ops = time_ops(torch, E, prim, n)
+        del prim
+        torch.cuda.empty_cache()
+
+    e2e = None
+    if not args.no_e2e:
+        import numpy as np
+
+        host = torch.empty((5, n0, n0, n0), dtype=torch.float64, pin_memory=True)
+        out = torch.empty((5, n0, n0, n0), dtype=torch.float64, pin_memory=True)
+        src = random_prim_device(torch, n0, n0, n0, seed=2)
+        host.copy_(src)
+        del src
+        torch.cuda.synchronize()
+        with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, stream=stream) as sim2:
+            sim2.set_prim(host)  # warm-up
+            sim2.advance(1)
+            sim2.get_state(prim=out)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                sim2.set_prim(host)
+                sim2.advance(1)
+                sim2.get_state(prim=out)
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
+        nbytes = 5 * n0 ** 3 * 8
+        e2e = {"value": world * interior * args.e2e_steps / el / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "how": "per step: eulr_sim_set_prim_f64 from pinned host prim (H2D + prim_to_cons + dt), "
+                      "eulr_sim_advance(1), eulr_sim_get_state_f64 of prim to pinned host (D2H); wall clock"}
+        del host, out
+        _ = np
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cpu = cpu_baseline(n, args.cpu_seconds)
+        cpu.pop("_np", None)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"fused Euler step, {n}^3 interior ({n0}^3 with ghosts), seeded random state "
+                                   "(rho, p log-uniform [0.1,10], u ~ N(0,1)), gamma 1.4, CFL 0.4",
+                       "n": n, "precision": "f64", "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (5.4 GB per bundle); no flush"},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "operators": ops,
+            "status": status,
+            "sim": {"t": t_sim, "steps_taken": nsteps},
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,197 @@
+// Device-side building blocks shared by the Euler kernels (sm_103a).
+//
+// Two arithmetic styles are used:
+//  * "exact" helpers (mul_rn, add_rn, ...) issue one IEEE-rounded operation
+//    each and never contract into FMA.  The pointwise operators use them so
+//    that their results are bit-identical to the reference operators, which
+//    are written as separately rounded products and sums.
+//  * plain C++ arithmetic, which nvcc contracts into FMAs.  The flux kernels
+//    use it: every face is solved once instead of twice, shared reciprocals
+//    replace divisions, and the results agree with the reference to a few
+//    units in the last place per step.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace eulr {
+
+template <class T>
+struct Bundle {
+    T* f[5];
+};
+
+template <class T>
+struct CBundle {
+    const T* f[5];
+};
+
+// Grid extents and strides of a layout_left block (i fastest).
+struct Geom {
+    int n0, n1, n2;
+    long long s1; // n0
+    long long s2; // n0 * n1
+    __host__ __device__ long long ncell() const { return s2 * n2; }
+    __host__ __device__ long long at(int i, int j, int k) const { return i + s1 * j + s2 * k; }
+};
+
+inline Geom make_geom(int n0, int n1, int n2)
+{
+    Geom g;
+    g.n0 = n0;
+    g.n1 = n1;
+    g.n2 = n2;
+    g.s1 = n0;
+    g.s2 = static_cast<long long>(n0) * n1;
+    return g;
+}
+
+// ------------------------------------------------ separately rounded ops
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rcp_rn(double a) { return __drcp_rn(a); }
+__device__ __forceinline__ float rcp_rn(float a) { return __frcp_rn(a); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float sqrt_rn(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double abs_(double a) { return fabs(a); }
+__device__ __forceinline__ float abs_(float a) { return fabsf(a); }
+
+// Correctly rounded x / y given r = RN(1/y): q0 = RN(x r) is within one ulp
+// of x/y, the remainder x - q0 y is exact through one FMA, and
+// RN(q0 + rem r) is the correctly rounded quotient (Markstein's correction
+// step; P. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  Valid away from
+// overflow and underflow, which the Euler states here never approach.
+template <class T>
+__device__ __forceinline__ T div_by_rcp(T x, T y, T r)
+{
+    T const q0 = mul_rn(x, r);
+    T const rem = fma_rn(-q0, y, x);
+    return fma_rn(rem, r, q0);
+}
+
+// Non-negative values ordered as their bit patterns; NaN maps to 0 so that it
+// never wins a max (the reference's Kokkos::min over 1/invdt skips NaN).
+__device__ __forceinline__ unsigned long long order_bits(double v)
+{
+    return (v >= 0.0) ? static_cast<unsigned long long>(__double_as_longlong(v)) : 0ull;
+}
+__device__ __forceinline__ unsigned long long order_bits(float v)
+{
+    return order_bits(static_cast<double>(v));
+}
+
+template <class T>
+__device__ __forceinline__ T warp_max(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T const w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (w > v) ? w : v;
+    }
+    return v;
+}
+
+// cons_to_prim of one cell, bit-identical to cons_to_prim.hpp:20-32 with
+// kinetic_energy(cons) (euler_arrays.hpp:44-48), PerfectGas::pressure
+// (perfect_gas.hpp:25-28) and to_prim (euler_arrays.hpp:66-75):
+//   ke = ((m.m)/d)/2, p = (gamma-1)*(e-ke), u_i = m_i * (1/d).
+// Both quotients come from one reciprocal of d (div_by_rcp).
+template <class T>
+__device__ __forceinline__ void cons_to_prim_exact(T d, T e, T m0, T m1, T m2, T gm1, T& p, T& u0, T& u1, T& u2)
+{
+    T const r = rcp_rn(d);
+    T const mm = add_rn(add_rn(mul_rn(m0, m0), mul_rn(m1, m1)), mul_rn(m2, m2));
+    T const ke = mul_rn(div_by_rcp(mm, d, r), T(0.5));
+    p = mul_rn(gm1, sub_rn(e, ke));
+    u0 = mul_rn(m0, r);
+    u1 = mul_rn(m1, r);
+    u2 = mul_rn(m2, r);
+}
+
+// (c + |u0|)/dx0 + (c + |u1|)/dx1 + (c + |u2|)/dx2 of one cell with
+// c = sqrt((gamma p)/d), bit-identical to time_step.hpp:28-33 and
+// perfect_gas.hpp:15-18 (ix_d = 1/dx_d computed by the caller in T).
+template <class T>
+__device__ __forceinline__ T cell_invdt_exact(T d, T p, T u0, T u1, T u2, T gamma, T ix0, T ix1, T ix2)
+{
+    T const cs = sqrt_rn(div_rn(mul_rn(gamma, p), d));
+    T const c0 = add_rn(cs, abs_(u0));
+    T const c1 = add_rn(cs, abs_(u1));
+    T const c2 = add_rn(cs, abs_(u2));
+    return add_rn(add_rn(mul_rn(c0, ix0), mul_rn(c1, ix1)), mul_rn(c2, ix2));
+}
+
+// ------------------------------------------------------------------ HLLC
+// One side of a face in the face's frame: normal velocity un, tangential
+// velocities ut1/ut2 (in the cyclic order of the axes after the normal), sound
+// speed c and total energy density e.
+template <class T>
+struct Side {
+    T d, p, un, ut1, ut2, c, e;
+};
+
+template <class T>
+struct Flux {
+    T d, e, n, t1, t2;
+};
+
+// HLLC flux of hllc::operator() (euler_operators/hllc.hpp:50-105) in the face
+// frame.  Wave speeds (:64-68), acoustic star state (:70-76), upwind side by
+// the sign of ustar (:78-79), supersonic test S_L*S_R > 0 (:84-85), star
+// density and energy (:86-88) and the flux (:90-102).  The two divisions by
+// (S - un_o) and (S - ustar) of the reference share one reciprocal: they have
+// the same denominator in the subsonic case, and in the supersonic case the
+// reference's ratio (S-un)/(S-un) is exactly 1 and its energy correction is
+// exactly 0, which is what the select below produces.
+template <class T>
+__device__ __forceinline__ Flux<T> hllc_flux(Side<T> const& L, Side<T> const& R)
+{
+    T const cmax = fmax(L.c, R.c);
+    T const S_L = fmin(L.un, R.un) - cmax;
+    T const S_R = fmax(L.un, R.un) + cmax;
+
+    T const rc_L = L.d * (S_L - L.un);
+    T const rc_R = R.d * (S_R - R.un);
+
+    T const ustar = (R.p - L.p + rc_L * L.un - rc_R * R.un) / (rc_L - rc_R);
+    T const pstar = T(0.5) * (L.p + R.p + rc_L * (ustar - L.un) + rc_R * (ustar - R.un));
+
+    bool const left = ustar > T(0);
+    T const S = left ? S_L : S_R;
+    T const qd = left ? L.d : R.d;
+    T const qp = left ? L.p : R.p;
+    T const qun = left ? L.un : R.un;
+    T const qut1 = left ? L.ut1 : R.ut1;
+    T const qut2 = left ? L.ut2 : R.ut2;
+    T const qe = left ? L.e : R.e;
+
+    bool const supersonic = S_L * S_R > T(0);
+    T const inv = T(1) / (S - ustar);
+    T const ratio = (S - qun) * inv;
+    T const d_star = ratio * qd;
+    T const e_star = ratio * qe + (pstar * ustar - qp * qun) * inv;
+
+    T const un_o = supersonic ? qun : ustar;
+    T const ptot_o = supersonic ? qp : pstar;
+    T const d_o = supersonic ? qd : d_star;
+    T const e_o = supersonic ? qe : e_star;
+
+    Flux<T> f;
+    f.d = d_o * un_o;
+    f.e = (e_o + ptot_o) * un_o;
+    f.n = f.d * un_o + ptot_o;
+    f.t1 = f.d * qut1;
+    f.t2 = f.d * qut2;
+    return f;
+}
+
+} // namespace eulr

@@ -1,0 +1,501 @@
+// Godunov/HLLC flux kernels (sm_103a): the per-operator godunov and the fused
+// simulation step share one z-marching tile engine.
+//
+// Work decomposition: the interior [1,n0-1) x [1,n1-1) x [1,n2-1) is cut into
+// TX x TY columns and each column into chunks of kchunk planes; a persistent
+// grid of CTAs walks the (tile, chunk) items round-robin.  A CTA marches up
+// its chunk one plane at a time with a ring of plane slots in shared memory,
+// each slot holding the 7 face inputs (d, p, u0, u1, u2, c, e) of a
+// (TX+2) x (TY+2) plane with its one-cell halo.  Per plane:
+//   1. face phase -- every x face and y face of plane k and every z face
+//      between planes k and k+1 is solved ONCE (the reference solves each
+//      interior face twice, once from each side, godunov.hpp:48-82); the
+//      808 faces of a 32x8 tile are spread linearly over the 256 threads,
+//      97% lane occupancy, and fluxes go to shared memory in global axes;
+//   2. cell phase -- each thread owns one column cell, sums
+//      ds_d (F_R - F_L) over the three axes in the reference's order and
+//      applies cons -= dt/dv * flux (godunov.hpp:84-90).  The z face below
+//      the cell is carried in registers from the previous plane.
+// The fused step then finishes the cell on chip: cons_to_prim, sound speed
+// and the next step's CFL max-wavespeed, reduced warp -> block -> one
+// atomicMax per CTA, so dt never leaves the device.
+#include "euler_device.cuh"
+#include "kernels.h"
+
+#include <cfloat>
+
+namespace eulr {
+
+namespace {
+
+constexpr int kFields = 7; // d, p, u0, u1, u2, c, e
+
+template <class T, int TX, int TY, int NSLOT>
+struct TileLayout {
+    static constexpr int HX = TX + 2;
+    static constexpr int HY = TY + 2;
+    static constexpr int PLANE = HX * HY;
+    static constexpr int NFX = (TX + 1) * TY;
+    static constexpr int NFY = TX * (TY + 1);
+    static constexpr int NFZ = TX * TY;
+    static constexpr int NFACE = NFX + NFY + NFZ;
+    static constexpr int NT = TX * TY;
+    // shared memory in T elements
+    static constexpr int Q_ELEMS = NSLOT * kFields * PLANE;
+    static constexpr int FX_OFF = Q_ELEMS;
+    static constexpr int FY_OFF = FX_OFF + 5 * NFX;
+    static constexpr int FZ_OFF = FY_OFF + 5 * NFY;
+    static constexpr int ELEMS = FZ_OFF + 5 * NFZ;
+    static constexpr size_t BYTES = sizeof(T) * static_cast<size_t>(ELEMS);
+};
+
+template <class T, int TX, int TY, int NSLOT>
+__device__ __forceinline__ T* slot_field(T* smem, int slot, int field)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    return smem + (slot * kFields + field) * L::PLANE;
+}
+
+// Stage plane k of the tile whose first interior cell is (i0, j0) into `slot`.
+// Godunov mode derives c and e from prim; step mode reads the stored sound
+// speed and the conservative energy.  Cells outside the array get a benign
+// uniform state; no face touching them is ever used.
+template <class T, int TX, int TY, int NSLOT, int MODE>
+__device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> const& p, int i0, int j0, int k)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    T* q = slot_field<T, TX, TY, NSLOT>(smem, slot, 0);
+    for (int c = threadIdx.x; c < L::PLANE; c += L::NT) {
+        int const hx = c % L::HX;
+        int const hy = c / L::HX;
+        int const i = i0 - 1 + hx;
+        int const j = j0 - 1 + hy;
+        T d = T(1), pr = T(1), u0 = T(0), u1 = T(0), u2 = T(0), cs = T(1), e = T(2.5);
+        if (i < p.g.n0 && j < p.g.n1) {
+            long long const o = p.g.at(i, j, k);
+            d = __ldg(p.prim.f[0] + o);
+            pr = __ldg(p.prim.f[1] + o);
+            u0 = __ldg(p.prim.f[2] + o);
+            u1 = __ldg(p.prim.f[3] + o);
+            u2 = __ldg(p.prim.f[4] + o);
+            if (MODE == kModeStep) {
+                cs = __ldg(p.cs + o);
+                e = __ldg(p.cons_in.f[1] + o);
+            } else {
+                T const r = T(1) / d;
+                cs = sqrt(p.gamma * pr * r);
+                e = pr * p.inv_gm1 + T(0.5) * d * (u0 * u0 + u1 * u1 + u2 * u2);
+            }
+        }
+        q[0 * L::PLANE + c] = d;
+        q[1 * L::PLANE + c] = pr;
+        q[2 * L::PLANE + c] = u0;
+        q[3 * L::PLANE + c] = u1;
+        q[4 * L::PLANE + c] = u2;
+        q[5 * L::PLANE + c] = cs;
+        q[6 * L::PLANE + c] = e;
+    }
+}
+
+template <class T, int PLANE>
+__device__ __forceinline__ Side<T> load_side(T const* q, int c, int dir)
+{
+    Side<T> s;
+    s.d = q[0 * PLANE + c];
+    s.p = q[1 * PLANE + c];
+    s.un = q[(2 + dir) * PLANE + c];
+    s.ut1 = q[(2 + (dir + 1) % 3) * PLANE + c];
+    s.ut2 = q[(2 + (dir + 2) % 3) * PLANE + c];
+    s.c = q[5 * PLANE + c];
+    s.e = q[6 * PLANE + c];
+    return s;
+}
+
+template <class T>
+__device__ __forceinline__ void store_flux(T* out, int stride, int idx, int dir, Flux<T> const& f)
+{
+    out[0 * stride + idx] = f.d;
+    out[1 * stride + idx] = f.e;
+    out[(2 + dir) * stride + idx] = f.n;
+    out[(2 + (dir + 1) % 3) * stride + idx] = f.t1;
+    out[(2 + (dir + 2) % 3) * stride + idx] = f.t2;
+}
+
+template <class T, int TX, int TY, int NSLOT, int MODE>
+__global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(smem_raw);
+    T* fx = smem + L::FX_OFF;
+    T* fy = smem + L::FY_OFF;
+    T* fz = smem + L::FZ_OFF;
+
+    T dtodv = p.dtodv;
+    if (p.dt_dev != nullptr) {
+        T const dtc = p.cfl * *p.dt_dev; // cfl * dt, euler_simulation.cpp:65
+        dtodv = dtc / p.dv;              // godunov.hpp:37
+    }
+    T const ds0 = p.ds0, ds1 = p.ds1, ds2 = p.ds2;
+
+    int const tid = threadIdx.x;
+    int const ti = tid % TX;
+    int const tj = tid / TX;
+    int const center = (tj + 1) * L::HX + ti + 1;
+
+    T wmax = T(0);
+    bool bad = false;
+
+    int const tiles_xy = p.tiles_x * p.tiles_y;
+    for (int w = blockIdx.x; w < p.nwork; w += gridDim.x) {
+        int const tx = w % p.tiles_x;
+        int const ty = (w / p.tiles_x) % p.tiles_y;
+        int const kc = w / tiles_xy;
+        int const i0 = 1 + tx * TX;
+        int const j0 = 1 + ty * TY;
+        int const kb = 1 + kc * p.kchunk;
+        int const ke = min(kb + p.kchunk, p.g.n2 - 1);
+        int const i = i0 + ti;
+        int const j = j0 + tj;
+        bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
+
+        __syncthreads(); // previous item's readers of the slots are done
+        load_plane<T, TX, TY, NSLOT, MODE>(smem, 0, p, i0, j0, kb - 1);
+        load_plane<T, TX, TY, NSLOT, MODE>(smem, 1, p, i0, j0, kb);
+        __syncthreads();
+        // z face below the chunk's first plane, kept in registers in global
+        // axes (the z face frame has n = mx2, t1 = mx0, t2 = mx1)
+        T zlo[5];
+        {
+            Flux<T> const f0 = hllc_flux(load_side<T, L::PLANE>(slot_field<T, TX, TY, NSLOT>(smem, 0, 0), center, 2),
+                                         load_side<T, L::PLANE>(slot_field<T, TX, TY, NSLOT>(smem, 1, 0), center, 2));
+            zlo[0] = f0.d;
+            zlo[1] = f0.e;
+            zlo[2] = f0.t1;
+            zlo[3] = f0.t2;
+            zlo[4] = f0.n;
+        }
+        __syncthreads(); // slot 0 is refilled by the first plane of the loop
+
+        for (int k = kb; k < ke; ++k) {
+            int const cur = (k - kb + 1) % NSLOT;
+            int const nxt = (k - kb + 2) % NSLOT;
+            // prefetch this cell's conservative state
+            T u[5];
+            long long const o = p.g.at(i, j, k);
+            if (own) {
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    u[f] = p.cons_in.f[f][o];
+                }
+            }
+            load_plane<T, TX, TY, NSLOT, MODE>(smem, nxt, p, i0, j0, k + 1);
+            __syncthreads();
+
+            // ---- face phase
+            T const* qc = slot_field<T, TX, TY, NSLOT>(smem, cur, 0);
+            T const* qn = slot_field<T, TX, TY, NSLOT>(smem, nxt, 0);
+            for (int f = tid; f < L::NFACE; f += L::NT) {
+                if (f < L::NFX) {
+                    int const fj = f / (TX + 1);
+                    int const fi = f % (TX + 1);
+                    int const a = (fj + 1) * L::HX + fi;
+                    store_flux(fx, L::NFX, f, 0,
+                               hllc_flux(load_side<T, L::PLANE>(qc, a, 0), load_side<T, L::PLANE>(qc, a + 1, 0)));
+                } else if (f < L::NFX + L::NFY) {
+                    int const g = f - L::NFX;
+                    int const fj = g / TX;
+                    int const fi = g % TX;
+                    int const a = fj * L::HX + fi + 1;
+                    store_flux(fy, L::NFY, g, 1,
+                               hllc_flux(load_side<T, L::PLANE>(qc, a, 1), load_side<T, L::PLANE>(qc, a + L::HX, 1)));
+                } else {
+                    int const g = f - L::NFX - L::NFY;
+                    int const fj = g / TX;
+                    int const fi = g % TX;
+                    int const a = (fj + 1) * L::HX + fi + 1;
+                    store_flux(fz, L::NFZ, g, 2,
+                               hllc_flux(load_side<T, L::PLANE>(qc, a, 2), load_side<T, L::PLANE>(qn, a, 2)));
+                }
+            }
+            __syncthreads();
+
+            // ---- cell phase
+            T fza[5];
+            fza[0] = fz[0 * L::NFZ + tid];
+            fza[1] = fz[1 * L::NFZ + tid];
+            fza[2] = fz[2 * L::NFZ + tid];
+            fza[3] = fz[3 * L::NFZ + tid];
+            fza[4] = fz[4 * L::NFZ + tid];
+            if (own) {
+                int const xl = tj * (TX + 1) + ti;
+                int const yb = tj * TX + ti;
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    T const ax = fx[f * L::NFX + xl + 1] - fx[f * L::NFX + xl];
+                    T const ay = fy[f * L::NFY + yb + TX] - fy[f * L::NFY + yb];
+                    T const az = fza[f] - zlo[f];
+                    T acc = ds0 * ax;
+                    acc = acc + ds1 * ay;
+                    acc = acc + ds2 * az;
+                    u[f] = u[f] - dtodv * acc;
+                }
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    p.cons_out.f[f][o] = u[f];
+                }
+                if (MODE == kModeStep) {
+                    T const r = T(1) / u[0];
+                    T const v0 = u[2] * r;
+                    T const v1 = u[3] * r;
+                    T const v2 = u[4] * r;
+                    T const ke_ = T(0.5) * r * (u[2] * u[2] + u[3] * u[3] + u[4] * u[4]);
+                    T const pr = p.gm1 * (u[1] - ke_);
+                    T const cs = sqrt(p.gamma * pr * r);
+                    p.prim_out.f[0][o] = u[0];
+                    p.prim_out.f[1][o] = pr;
+                    p.prim_out.f[2][o] = v0;
+                    p.prim_out.f[3][o] = v1;
+                    p.prim_out.f[4][o] = v2;
+                    p.cs_out[o] = cs;
+                    T const invdt = (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
+                    wmax = (invdt > wmax) ? invdt : wmax;
+                    bad |= !(u[0] > T(0)) || !(pr > T(0)) || !(invdt <= T(3.0e38));
+                }
+            }
+            // the z face above becomes the next plane's z face below
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                zlo[f] = fza[f];
+            }
+        }
+    }
+
+    if (MODE == kModeStep) {
+        __shared__ T warp_best[TX * TY / 32];
+        __shared__ int any_bad;
+        if (tid == 0) {
+            any_bad = 0;
+        }
+        wmax = warp_max(wmax);
+        __syncthreads();
+        if ((tid & 31) == 0) {
+            warp_best[tid >> 5] = wmax;
+        }
+        if (bad) {
+            any_bad = 1;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            T b = warp_best[0];
+#pragma unroll
+            for (int wv = 1; wv < TX * TY / 32; ++wv) {
+                b = (warp_best[wv] > b) ? warp_best[wv] : b;
+            }
+            atomicMax(p.wmax, order_bits(b));
+            if (any_bad) {
+                atomicOr(p.status, 1);
+            }
+        }
+    }
+}
+
+// Ghost shell of the step's output: cons copied, prim = cons_to_prim(cons)
+// (bit-identical to the reference's cons_to_prim over ghosts,
+// cons_to_prim.hpp:26-27), sound speed and CFL contribution.
+template <class T>
+__global__ void __launch_bounds__(256) ghost_shell_kernel(GhostParams<T> p)
+{
+    Geom const g = p.g;
+    bool const all = (g.n0 < 3) || (g.n1 < 3) || (g.n2 < 3);
+    long long const plane = g.s2;
+    long long const ring = 2LL * g.n0 + 2LL * (g.n1 - 2);
+    long long const total = all ? g.ncell() : 2 * plane + ring * (g.n2 - 2);
+    T wmax = T(0);
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < total;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        long long o;
+        if (all) {
+            o = c;
+        } else if (c < 2 * plane) {
+            o = (c < plane) ? c : c - plane + plane * (g.n2 - 1);
+        } else {
+            long long const r0 = c - 2 * plane;
+            int const k = 1 + static_cast<int>(r0 / ring);
+            int const r = static_cast<int>(r0 % ring);
+            int i, j;
+            if (r < g.n0) {
+                i = r;
+                j = 0;
+            } else if (r < 2 * g.n0) {
+                i = r - g.n0;
+                j = g.n1 - 1;
+            } else {
+                int const r2 = r - 2 * g.n0;
+                j = 1 + r2 / 2;
+                i = (r2 & 1) ? g.n0 - 1 : 0;
+            }
+            o = g.at(i, j, k);
+        }
+        T const d = p.cons_in.f[0][o];
+        T const e = p.cons_in.f[1][o];
+        T const m0 = p.cons_in.f[2][o];
+        T const m1 = p.cons_in.f[3][o];
+        T const m2 = p.cons_in.f[4][o];
+        T pr, u0, u1, u2;
+        cons_to_prim_exact(d, e, m0, m1, m2, p.gm1, pr, u0, u1, u2);
+        p.cons_out.f[0][o] = d;
+        p.cons_out.f[1][o] = e;
+        p.cons_out.f[2][o] = m0;
+        p.cons_out.f[3][o] = m1;
+        p.cons_out.f[4][o] = m2;
+        p.prim_out.f[0][o] = d;
+        p.prim_out.f[1][o] = pr;
+        p.prim_out.f[2][o] = u0;
+        p.prim_out.f[3][o] = u1;
+        p.prim_out.f[4][o] = u2;
+        p.cs_out[o] = sqrt_rn(div_rn(mul_rn(p.gamma, pr), d));
+        T const v = cell_invdt_exact(d, pr, u0, u1, u2, p.gamma, p.invdx0, p.invdx1, p.invdx2);
+        wmax = (v > wmax) ? v : wmax;
+    }
+    __shared__ T warp_best[8];
+    wmax = warp_max(wmax);
+    if ((threadIdx.x & 31) == 0) {
+        warp_best[threadIdx.x >> 5] = wmax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T b = warp_best[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            b = (warp_best[w] > b) ? warp_best[w] : b;
+        }
+        atomicMax(p.wmax, order_bits(b));
+    }
+}
+
+// Turns the max-wavespeed accumulator into the next step's dt
+// (time_step.hpp:34-39: min over cells of 1/invdt == 1/max invdt), adds the
+// step just taken to the simulated time and clears the accumulator.
+template <class T>
+__global__ void finalize_dt_kernel(SimScalars* s, T cfl, int add_time)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (add_time) {
+            s->t += static_cast<double>(cfl * static_cast<T>(s->dt));
+            s->steps += 1;
+        }
+        T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(s->wmax)));
+        T const dt = (m > T(0)) ? rcp_rn(m) : (sizeof(T) == 8 ? T(DBL_MAX) : T(FLT_MAX));
+        s->dt = static_cast<double>(dt);
+        s->wmax = 0ull;
+    }
+}
+
+// Opts the kernel into its dynamic shared memory size and returns its
+// resident CTAs per SM.  Called outside any stream capture (by the entry
+// points before they enqueue work), and cheap to repeat.
+template <class T, int TX, int TY, int NSLOT, int MODE>
+cudaError_t configure_flux_impl(int* per_sm)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    auto kern = flux_tile_kernel<T, TX, TY, NSLOT, MODE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(L::BYTES));
+    if (e != cudaSuccess) {
+        return e;
+    }
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, L::NT, L::BYTES);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    *per_sm = n < 1 ? 1 : n;
+    return cudaSuccess;
+}
+
+template <class T, int TX, int TY, int NSLOT, int MODE>
+cudaError_t launch_flux_impl(FluxParams<T> p, int sms, cudaStream_t s)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    auto kern = flux_tile_kernel<T, TX, TY, NSLOT, MODE>;
+    int const per_sm = p.per_sm > 0 ? p.per_sm : 1;
+    int const ix = p.g.n0 - 2;
+    int const iy = p.g.n1 - 2;
+    int const iz = p.g.n2 - 2;
+    if (ix <= 0 || iy <= 0 || iz <= 0) {
+        return cudaSuccess; // no interior cell
+    }
+    p.tiles_x = (ix + TX - 1) / TX;
+    p.tiles_y = (iy + TY - 1) / TY;
+    if (p.kchunk <= 0) {
+        p.kchunk = 32;
+    }
+    int const kchunks = (iz + p.kchunk - 1) / p.kchunk;
+    long long const nwork = static_cast<long long>(p.tiles_x) * p.tiles_y * kchunks;
+    p.nwork = static_cast<int>(nwork);
+    long long grid = static_cast<long long>(sms) * per_sm;
+    if (grid > nwork) {
+        grid = nwork;
+    }
+    kern<<<static_cast<int>(grid), L::NT, L::BYTES, s>>>(p);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+template <class T>
+cudaError_t configure_flux(int mode, int* per_sm)
+{
+    if (mode == kModeStep) {
+        return configure_flux_impl<T, 32, 8, 2, kModeStep>(per_sm);
+    }
+    return configure_flux_impl<T, 32, 8, 2, kModeGodunov>(per_sm);
+}
+
+template <class T>
+cudaError_t launch_flux(FluxParams<T> p, int mode, int sms, cudaStream_t s)
+{
+    if (mode == kModeStep) {
+        return launch_flux_impl<T, 32, 8, 2, kModeStep>(p, sms, s);
+    }
+    return launch_flux_impl<T, 32, 8, 2, kModeGodunov>(p, sms, s);
+}
+
+template <class T>
+cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s)
+{
+    Geom const& g = p.g;
+    long long total;
+    if (g.n0 < 3 || g.n1 < 3 || g.n2 < 3) {
+        total = g.ncell();
+    } else {
+        total = 2 * g.s2 + (2LL * g.n0 + 2LL * (g.n1 - 2)) * (g.n2 - 2);
+    }
+    long long blocks = (total + 255) / 256;
+    long long const cap = static_cast<long long>(sms) * 8;
+    if (blocks > cap) {
+        blocks = cap;
+    }
+    if (blocks < 1) {
+        blocks = 1;
+    }
+    ghost_shell_kernel<T><<<static_cast<int>(blocks), 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s)
+{
+    finalize_dt_kernel<T><<<1, 32, 0, s>>>(sc, cfl, add_time);
+    return cudaGetLastError();
+}
+
+template cudaError_t configure_flux<double>(int, int*);
+template cudaError_t configure_flux<float>(int, int*);
+template cudaError_t launch_flux<double>(FluxParams<double>, int, int, cudaStream_t);
+template cudaError_t launch_flux<float>(FluxParams<float>, int, int, cudaStream_t);
+template cudaError_t launch_ghost_shell<double>(GhostParams<double>, int, cudaStream_t);
+template cudaError_t launch_ghost_shell<float>(GhostParams<float>, int, cudaStream_t);
+template cudaError_t launch_finalize_dt<double>(SimScalars*, double, int, cudaStream_t);
+template cudaError_t launch_finalize_dt<float>(SimScalars*, float, int, cudaStream_t);
+
+} // namespace eulr

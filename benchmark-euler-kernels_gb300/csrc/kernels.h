@@ -1,0 +1,84 @@
+// Host-side launch interface of the Euler kernels (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "euler_device.cuh"
+
+namespace eulr {
+
+constexpr int kModeGodunov = 0; // per-operator godunov: cons updated in place from prim
+constexpr int kModeStep = 1;    // fused step: ping-pong buffers, next-step CFL reduction
+
+// Device scalars of a simulation.
+struct SimScalars {
+    unsigned long long wmax; // max invdt of the state being produced (ordered bits of a double)
+    double dt;               // time_step() of the current state (before the CFL factor)
+    double t;                // simulated time: sum of cfl*dt over the steps taken
+    long long steps;         // steps taken
+    int status;              // bit 0: a cell became non-finite or non-physical
+    int pad;
+};
+
+template <class T>
+struct FluxParams {
+    Geom g;
+    CBundle<T> prim;     // read (with halo)
+    const T* cs;         // step mode: stored sound speed of prim
+    CBundle<T> cons_in;  // read (centre; step mode also e with halo)
+    Bundle<T> cons_out;  // written (interior); may equal cons_in in godunov mode
+    Bundle<T> prim_out;  // step mode: cons_to_prim of the new state (interior)
+    T* cs_out;           // step mode: sound speed of the new state (interior)
+    T gamma, gm1, inv_gm1;
+    T ds0, ds1, ds2;     // face areas dx1*dx2, dx2*dx0, dx0*dx1
+    T dv;                // cell volume
+    T dtodv;             // dt/dv when dt_dev is null
+    const T* dt_dev;     // if set: dt/dv = (cfl * *dt_dev) / dv
+    T cfl;
+    T invdx0, invdx1, invdx2;
+    unsigned long long* wmax; // step mode: atomicMax of the next max invdt
+    int* status;              // step mode: set to 1 on a non-physical cell
+    int tiles_x, tiles_y, kchunk, nwork; // work decomposition (kchunk <= 0: default)
+    int per_sm;                          // resident CTAs per SM (from configure_flux)
+};
+
+template <class T>
+struct GhostParams {
+    Geom g;
+    CBundle<T> cons_in;
+    Bundle<T> cons_out;
+    Bundle<T> prim_out;
+    T* cs_out;
+    T gamma, gm1;
+    T invdx0, invdx1, invdx2;
+    unsigned long long* wmax;
+};
+
+template <class T>
+cudaError_t launch_init_implode(Bundle<T> prim, Geom g, double dx0, double dx1, double dx2, int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_prim_to_cons(CBundle<T> prim, Bundle<T> cons, long long n, T gm1, T rgm1, int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_cons_to_prim(CBundle<T> cons, Bundle<T> prim, long long n, T gm1, int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_time_step(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2, T* partials,
+                             int max_partials, unsigned int* counter, T* dt_out, int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2, unsigned long long* wmax,
+                             int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s);
+
+template <class T>
+cudaError_t configure_flux(int mode, int* per_sm);
+template <class T>
+cudaError_t launch_flux(FluxParams<T> p, int mode, int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s);
+
+cudaError_t launch_fma_probe(int kind, int blocks, int iters, float* sink, cudaStream_t s);
+cudaError_t launch_totals(CBundle<double> cons, Geom g, double* out5, int sms, cudaStream_t s);
+
+} // namespace eulr

@@ -1,0 +1,255 @@
+// Pointwise Euler operators and the CFL reduction (sm_103a).
+//
+// Each kernel restates one reference operator with separately rounded
+// operations in the reference's operand order, so the results are
+// bit-identical to euler_operators/*.hpp compiled without FMA contraction.
+// All of them are bound by the FP64 pipe on GB300 (1/64 of the FP32 rate),
+// not by HBM, so the only optimisation that matters is issuing fewer FP64
+// instructions: divisions by the loop-invariant gamma-1 use a precomputed
+// reciprocal plus one Markstein correction, and cons_to_prim derives both of
+// its quotients from one reciprocal of rho.
+#include "euler_device.cuh"
+#include "kernels.h"
+
+#include <cfloat>
+
+namespace eulr {
+
+// ------------------------------------------------------------ init_implode
+// init_implode.hpp:24-44.  Cell centres are computed in double (the literal 0.5
+// promotes (i-1) to double) and rounded to T, as in the reference's float
+// instantiation.
+template <class T>
+__global__ void __launch_bounds__(256) init_implode_kernel(Bundle<T> prim, Geom g, double dx0, double dx1, double dx2)
+{
+    long long const n = g.ncell();
+    T const radius2 = static_cast<T>(0.25 * 0.25);
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int const i = static_cast<int>(c % g.n0);
+        long long const jk = c / g.n0;
+        int const j = static_cast<int>(jk % g.n1);
+        int const k = static_cast<int>(jk / g.n1);
+        T const x0 = static_cast<T>(__dsub_rn(__dmul_rn(__dadd_rn(static_cast<double>(i - 1), 0.5), dx0), 0.5));
+        T const x1 = static_cast<T>(__dsub_rn(__dmul_rn(__dadd_rn(static_cast<double>(j - 1), 0.5), dx1), 0.5));
+        T const x2 = static_cast<T>(__dsub_rn(__dmul_rn(__dadd_rn(static_cast<double>(k - 1), 0.5), dx2), 0.5));
+        T const r2 = add_rn(add_rn(mul_rn(x0, x0), mul_rn(x1, x1)), mul_rn(x2, x2));
+        bool const inside = r2 < radius2;
+        prim.f[0][c] = inside ? T(1) : T(0.125);
+        prim.f[1][c] = inside ? T(1) : T(0.14);
+        prim.f[2][c] = T(0);
+        prim.f[3][c] = T(0);
+        prim.f[4][c] = T(0);
+    }
+}
+
+// ------------------------------------------------------------ prim_to_cons
+// prim_to_cons.hpp:20-32 with to_cons (euler_arrays.hpp:56-64):
+//   e = d*((u0*u0 + u1*u1) + u2*u2)/2 + p/(gamma-1),  m_i = d*u_i.
+template <class T>
+__global__ void __launch_bounds__(256) prim_to_cons_kernel(CBundle<T> prim, Bundle<T> cons, long long n, T gm1, T rgm1)
+{
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        T const d = prim.f[0][c];
+        T const p = prim.f[1][c];
+        T const u0 = prim.f[2][c];
+        T const u1 = prim.f[3][c];
+        T const u2 = prim.f[4][c];
+        T const int_e = div_by_rcp(p, gm1, rgm1);
+        T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
+        cons.f[0][c] = d;
+        cons.f[1][c] = add_rn(ke, int_e);
+        cons.f[2][c] = mul_rn(d, u0);
+        cons.f[3][c] = mul_rn(d, u1);
+        cons.f[4][c] = mul_rn(d, u2);
+    }
+}
+
+// ------------------------------------------------------------ cons_to_prim
+// cons_to_prim.hpp:20-32 with kinetic_energy(cons) (euler_arrays.hpp:44-48),
+// PerfectGas::pressure and to_prim (euler_arrays.hpp:66-75):
+//   ke = ((m.m)/d)/2, p = (gamma-1)*(e-ke), u_i = m_i * (1/d).
+template <class T>
+__global__ void __launch_bounds__(256) cons_to_prim_kernel(CBundle<T> cons, Bundle<T> prim, long long n, T gm1)
+{
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        T const d = cons.f[0][c];
+        T p, u0, u1, u2;
+        cons_to_prim_exact(d, cons.f[1][c], cons.f[2][c], cons.f[3][c], cons.f[4][c], gm1, p, u0, u1, u2);
+        prim.f[0][c] = d;
+        prim.f[1][c] = p;
+        prim.f[2][c] = u0;
+        prim.f[3][c] = u1;
+        prim.f[4][c] = u2;
+    }
+}
+
+// --------------------------------------------------------------- time_step
+// time_step.hpp:22-39.  The reference takes min over cells of 1/invdt; since
+// correctly rounded division is monotonic, min_c RN(1/x_c) = RN(1/max_c x_c),
+// so the kernel reduces max(invdt) (exact, order-free) and divides once.
+// NaN never wins (the reference's Kokkos::min skips it) and an all-zero grid
+// returns the reduction identity T's max, as the reference's Min reducer does.
+template <class T>
+__global__ void __launch_bounds__(256) time_step_kernel(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2,
+                                                        T* partials, unsigned int* counter, T* dt_out)
+{
+    T local = T(0);
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        T const v = cell_invdt_exact(prim.f[0][c], prim.f[1][c], prim.f[2][c], prim.f[3][c], prim.f[4][c], gamma,
+                                     ix0, ix1, ix2);
+        local = (v > local) ? v : local;
+    }
+    __shared__ T warp_best[8];
+    __shared__ bool is_last;
+    local = warp_max(local);
+    if ((threadIdx.x & 31) == 0) {
+        warp_best[threadIdx.x >> 5] = local;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T b = warp_best[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            b = (warp_best[w] > b) ? warp_best[w] : b;
+        }
+        partials[blockIdx.x] = b;
+        __threadfence();
+        unsigned int const done = atomicAdd(counter, 1u);
+        is_last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (is_last) {
+        // Last block to finish: fold the per-block maxima and publish dt.
+        __threadfence();
+        T b = T(0);
+        for (unsigned int w = threadIdx.x; w < gridDim.x; w += blockDim.x) {
+            T const v = __ldcg(&partials[w]);
+            b = (v > b) ? v : b;
+        }
+        b = warp_max(b);
+        if ((threadIdx.x & 31) == 0) {
+            warp_best[threadIdx.x >> 5] = b;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            T m = warp_best[0];
+            for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+                m = (warp_best[w] > m) ? warp_best[w] : m;
+            }
+            *dt_out = (m > T(0)) ? rcp_rn(m) : (sizeof(T) == 8 ? T(DBL_MAX) : T(FLT_MAX));
+            *counter = 0u;
+        }
+    }
+}
+
+// Per-cell invdt max into an ordered-bits accumulator (used by the
+// simulation's initial reduction).
+template <class T>
+__global__ void __launch_bounds__(256) invdt_max_kernel(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2,
+                                                        unsigned long long* wmax)
+{
+    T local = T(0);
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        T const v = cell_invdt_exact(prim.f[0][c], prim.f[1][c], prim.f[2][c], prim.f[3][c], prim.f[4][c], gamma,
+                                     ix0, ix1, ix2);
+        local = (v > local) ? v : local;
+    }
+    __shared__ T warp_best[8];
+    local = warp_max(local);
+    if ((threadIdx.x & 31) == 0) {
+        warp_best[threadIdx.x >> 5] = local;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T b = warp_best[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            b = (warp_best[w] > b) ? warp_best[w] : b;
+        }
+        atomicMax(wmax, order_bits(b));
+    }
+}
+
+// Sound speed sqrt((gamma p)/d) of every cell (perfect_gas.hpp:15-18).
+template <class T>
+__global__ void __launch_bounds__(256) sound_speed_kernel(CBundle<T> prim, T* cs, long long n, T gamma)
+{
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        cs[c] = sqrt_rn(div_rn(mul_rn(gamma, prim.f[1][c]), prim.f[0][c]));
+    }
+}
+
+// ------------------------------------------------------------------ launch
+static int grid_for(long long n, int sms)
+{
+    long long const blocks = (n + 255) / 256;
+    long long const cap = static_cast<long long>(sms) * 8;
+    return static_cast<int>(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
+}
+
+template <class T>
+cudaError_t launch_init_implode(Bundle<T> prim, Geom g, double dx0, double dx1, double dx2, int sms, cudaStream_t s)
+{
+    init_implode_kernel<T><<<grid_for(g.ncell(), sms), 256, 0, s>>>(prim, g, dx0, dx1, dx2);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_prim_to_cons(CBundle<T> prim, Bundle<T> cons, long long n, T gm1, T rgm1, int sms, cudaStream_t s)
+{
+    prim_to_cons_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cons, n, gm1, rgm1);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_cons_to_prim(CBundle<T> cons, Bundle<T> prim, long long n, T gm1, int sms, cudaStream_t s)
+{
+    cons_to_prim_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(cons, prim, n, gm1);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_time_step(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2, T* partials,
+                             int max_partials, unsigned int* counter, T* dt_out, int sms, cudaStream_t s)
+{
+    int grid = grid_for(n, sms);
+    if (grid > max_partials) {
+        grid = max_partials;
+    }
+    time_step_kernel<T><<<grid, 256, 0, s>>>(prim, n, gamma, ix0, ix1, ix2, partials, counter, dt_out);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2, unsigned long long* wmax,
+                             int sms, cudaStream_t s)
+{
+    invdt_max_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, n, gamma, ix0, ix1, ix2, wmax);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s)
+{
+    sound_speed_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cs, n, gamma);
+    return cudaGetLastError();
+}
+
+#define EULR_INSTANTIATE_POINTWISE(T)                                                                        \
+    template cudaError_t launch_init_implode<T>(Bundle<T>, Geom, double, double, double, int, cudaStream_t); \
+    template cudaError_t launch_prim_to_cons<T>(CBundle<T>, Bundle<T>, long long, T, T, int, cudaStream_t);  \
+    template cudaError_t launch_cons_to_prim<T>(CBundle<T>, Bundle<T>, long long, T, int, cudaStream_t);     \
+    template cudaError_t launch_time_step<T>(CBundle<T>, long long, T, T, T, T, T*, int, unsigned int*, T*,  \
+                                             int, cudaStream_t);                                             \
+    template cudaError_t launch_invdt_max<T>(CBundle<T>, long long, T, T, T, T, unsigned long long*, int,    \
+                                             cudaStream_t);                                                  \
+    template cudaError_t launch_sound_speed<T>(CBundle<T>, T*, long long, T, int, cudaStream_t);
+
+EULR_INSTANTIATE_POINTWISE(double)
+EULR_INSTANTIATE_POINTWISE(float)
+
+} // namespace eulr

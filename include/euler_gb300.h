@@ -1,0 +1,248 @@
+/*
+ * euler_gb300 -- C ABI of the GB300 (sm_103a) first-order Godunov/HLLC step
+ * for 3D compressible Euler.
+ *
+ * Every entry point takes plain device pointers and sizes, is asynchronous on
+ * the given CUDA stream unless stated otherwise, and returns EULR_SUCCESS (0)
+ * or a negative eulr_status code.  Nothing throws across this boundary.
+ *
+ * Data layout (the reference's, euler_operators/euler_arrays.hpp:77-85 and
+ * :228-236, simulations/euler_simulation.cpp:37-48): structure of arrays, one
+ * array per field, each a layout_left block (i fastest) of n0*n1*n2 cells,
+ * cell (i,j,k) at offset i + n0*(j + n1*k).  Grids carry one ghost layer on
+ * every face, so the interior is [1, n-1) along each axis.
+ *   prim fields: d (density), p (pressure), ux0, ux1, ux2 (velocity)
+ *   cons fields: d (density), e (total energy), mx0, mx1, mx2 (momentum)
+ * Field arrays must be 8-byte (double) / 4-byte (float) aligned device
+ * memory.  Sizes: n0, n1, n2 >= 1 and n0*n1*n2 < 2^31 (the reference indexes
+ * with int, benchmarks/index_type.hpp:4).
+ */
+#ifndef EULER_GB300_H
+#define EULER_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* eulr_stream_t;
+
+typedef enum eulr_status {
+    EULR_SUCCESS = 0,
+    EULR_ERR_INVALID_ARGUMENT = -1, /* null pointer, bad size or aliasing */
+    EULR_ERR_INVALID_VALUE = -2,    /* gamma <= 1, dx <= 0, cfl <= 0, non-finite scalar */
+    EULR_ERR_MISALIGNED = -3,       /* field pointer not aligned to its element size */
+    EULR_ERR_CUDA = -4,             /* a CUDA runtime call failed (see eulr_last_error) */
+    EULR_ERR_OUT_OF_MEMORY = -5,
+    EULR_ERR_TOO_LARGE = -6,        /* size beyond the supported maximum */
+    EULR_ERR_NONFINITE = -7,        /* the state became non-finite or non-physical */
+    EULR_ERR_NO_DEVICE = -8,
+    EULR_ERR_UNSUPPORTED = -9
+} eulr_status;
+
+/* Primitive-variable bundle (reference EulerPrimArrays, euler_arrays.hpp:77-85). */
+typedef struct eulr_prim_f64 {
+    double* d;
+    double* p;
+    double* ux0;
+    double* ux1;
+    double* ux2;
+} eulr_prim_f64;
+
+/* Conservative-variable bundle (reference EulerConsArrays, euler_arrays.hpp:228-236). */
+typedef struct eulr_cons_f64 {
+    double* d;
+    double* e;
+    double* mx0;
+    double* mx1;
+    double* mx2;
+} eulr_cons_f64;
+
+/* Read-only views (the reference's as_const, euler_arrays.hpp:98-104, 238-255). */
+typedef struct eulr_prim_cf64 {
+    const double* d;
+    const double* p;
+    const double* ux0;
+    const double* ux1;
+    const double* ux2;
+} eulr_prim_cf64;
+
+typedef struct eulr_cons_cf64 {
+    const double* d;
+    const double* e;
+    const double* mx0;
+    const double* mx1;
+    const double* mx2;
+} eulr_cons_cf64;
+
+/* real_t = float bundles (benchmarks/real_type.hpp:3). */
+typedef struct eulr_prim_f32 {
+    float* d;
+    float* p;
+    float* ux0;
+    float* ux1;
+    float* ux2;
+} eulr_prim_f32;
+
+typedef struct eulr_cons_f32 {
+    float* d;
+    float* e;
+    float* mx0;
+    float* mx1;
+    float* mx2;
+} eulr_cons_f32;
+
+typedef struct eulr_prim_cf32 {
+    const float* d;
+    const float* p;
+    const float* ux0;
+    const float* ux1;
+    const float* ux2;
+} eulr_prim_cf32;
+
+typedef struct eulr_cons_cf32 {
+    const float* d;
+    const float* e;
+    const float* mx0;
+    const float* mx1;
+    const float* mx2;
+} eulr_cons_cf32;
+
+/* ---------------------------------------------------------------- library */
+
+/* Library version as major*10000 + minor*100 + patch. */
+int eulr_version(void);
+
+/* Human-readable name of a status code (static storage). */
+const char* eulr_status_string(int status);
+
+/* Message of the last error raised on the calling thread (thread-local
+ * storage; empty string when none). */
+const char* eulr_last_error(void);
+
+/* ------------------------------------------------- per-operator entry points
+ * Drop-in replacements of the reference operators, with the reference's
+ * argument meaning.  Each launches on `stream` and returns without waiting. */
+
+/* init_implode (euler_operators/init_implode.hpp:7-45): sphere of radius 0.25
+ * centred on (0.5,0.5,0.5), cell centres ((i-1)+0.5)*dx - 0.5 (ghosts
+ * included); rho=1, p=1 inside, rho=0.125, p=0.14 outside, u=0.
+ * Bit-identical to the reference. */
+int eulr_init_implode_f64(eulr_prim_f64 prim, int n0, int n1, int n2, double dx0, double dx1, double dx2,
+                          eulr_stream_t stream);
+int eulr_init_implode_f32(eulr_prim_f32 prim, int n0, int n1, int n2, float dx0, float dx1, float dx2,
+                          eulr_stream_t stream);
+
+/* prim_to_cons (euler_operators/prim_to_cons.hpp:7-33) over all cells.
+ * Bit-identical to the reference. */
+int eulr_prim_to_cons_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int n1, int n2, double gamma,
+                          eulr_stream_t stream);
+int eulr_prim_to_cons_f32(eulr_prim_cf32 prim, eulr_cons_f32 cons, int n0, int n1, int n2, float gamma,
+                          eulr_stream_t stream);
+
+/* cons_to_prim (euler_operators/cons_to_prim.hpp:7-33) over all cells,
+ * ghosts included.  Bit-identical to the reference. */
+int eulr_cons_to_prim_f64(eulr_cons_cf64 cons, eulr_prim_f64 prim, int n0, int n1, int n2, double gamma,
+                          eulr_stream_t stream);
+int eulr_cons_to_prim_f32(eulr_cons_cf32 cons, eulr_prim_f32 prim, int n0, int n1, int n2, float gamma,
+                          eulr_stream_t stream);
+
+/* time_step (euler_operators/time_step.hpp:8-41): min over all cells of
+ * 1 / sum_d (c + |u_d|) / dx_d, written to the DEVICE scalar *dt_out (the
+ * CFL factor is applied by the caller, as in the reference).  The result is
+ * bit-identical to the reference.  Uses a per-device scratch buffer that the
+ * library allocates with cudaMalloc on the first call on each device and
+ * keeps until exit; calls on the same device and different streams must not
+ * overlap. */
+int eulr_time_step_f64(eulr_prim_cf64 prim, int n0, int n1, int n2, double gamma, double dx0, double dx1,
+                       double dx2, double* dt_out, eulr_stream_t stream);
+int eulr_time_step_f32(eulr_prim_cf32 prim, int n0, int n1, int n2, float gamma, float dx0, float dx1,
+                       float dx2, float* dt_out, eulr_stream_t stream);
+
+/* godunov (euler_operators/godunov.hpp:15-92): for interior cells,
+ * cons -= dt/dv * sum_d ds_d (F_{d,R} - F_{d,L}) with HLLC fluxes
+ * (euler_operators/hllc.hpp:50-105) from the read-only prim; cons is updated
+ * in place, ghosts untouched.  Each face is solved once.  prim and cons must
+ * not overlap.  Matches the reference within 1e-12 relative L-infinity. */
+int eulr_godunov_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int n1, int n2, double gamma, double dx0,
+                     double dx1, double dx2, double dt, eulr_stream_t stream);
+int eulr_godunov_f32(eulr_prim_cf32 prim, eulr_cons_f32 cons, int n0, int n1, int n2, float gamma, float dx0,
+                     float dx1, float dx2, float dt, eulr_stream_t stream);
+
+/* As eulr_godunov_f64 with the time step read on the device: the update uses
+ * dt = cfl * (*dt_dev), so a time_step -> godunov loop never copies dt to the
+ * host (simulations/euler_simulation.cpp:57-65). */
+int eulr_godunov_devdt_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int n1, int n2, double gamma,
+                           double dx0, double dx1, double dx2, const double* dt_dev, double cfl,
+                           eulr_stream_t stream);
+
+/* ------------------------------------------------ device-resident simulation
+ * A simulation owns its device state (two copies of prim, cons and sound
+ * speed for ping-pong, plus a few device scalars) and advances it with one
+ * fused kernel per step: the step of simulations/euler_simulation.cpp:56-68
+ * (dt = time_step(prim); godunov(cfl*dt); cons_to_prim) with the CFL
+ * reduction of the next step folded into the update, so dt never leaves the
+ * device. */
+typedef struct eulr_sim eulr_sim;
+
+typedef enum eulr_precision {
+    EULR_PRECISION_F64 = 0,  /* plain FP64 */
+    EULR_PRECISION_F32C = 1, /* FP32 state with compensated update */
+    EULR_PRECISION_F32 = 2   /* plain FP32 (real_t = float) */
+} eulr_precision;
+
+int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double dx0, double dx1, double dx2,
+                    double cfl, eulr_stream_t stream, eulr_sim** out);
+int eulr_sim_destroy(eulr_sim* sim);
+
+/* Load the state.  Pointers may be host or device memory (copies use
+ * cudaMemcpyDefault).  set_prim computes cons = prim_to_cons(prim), as the
+ * reference driver does after init (euler_simulation.cpp:50-51);
+ * set_state takes both bundles as they are. */
+int eulr_sim_set_prim_f64(eulr_sim* sim, eulr_prim_cf64 prim);
+int eulr_sim_set_state_f64(eulr_sim* sim, eulr_prim_cf64 prim, eulr_cons_cf64 cons);
+/* init_implode + prim_to_cons on the device. */
+int eulr_sim_init_implode(eulr_sim* sim);
+
+/* Advance nsteps steps (asynchronous; replays a CUDA graph). */
+int eulr_sim_advance(eulr_sim* sim, int nsteps);
+
+/* Copy the current state out (host or device destination); waits for the
+ * stream.  Either bundle pointer set may be all-NULL to skip it. */
+int eulr_sim_get_state_f64(eulr_sim* sim, eulr_prim_f64 prim, eulr_cons_f64 cons);
+
+/* Simulated time (sum of cfl*dt over the steps taken), the dt of the next
+ * step, and the number of steps taken; waits for the stream. */
+int eulr_sim_time(eulr_sim* sim, double* t, double* next_dt, long long* steps);
+
+/* EULR_SUCCESS, or EULR_ERR_NONFINITE once any cell produced a non-finite
+ * or non-positive density/pressure; waits for the stream. */
+int eulr_sim_status(eulr_sim* sim);
+
+/* Number of kernel launches one step issues (for launch accounting). */
+int eulr_sim_launches_per_step(eulr_sim* sim);
+
+/* Runs ONE step with CUDA events between its launches on the simulation's
+ * stream and returns the device time of each launch in milliseconds:
+ * ms[0] ghost shell, ms[1] fused flux/update kernel, ms[2] dt finalize.
+ * Synchronous; advances the state like eulr_sim_advance(sim, 1). */
+int eulr_sim_profile_step(eulr_sim* sim, float ms[3]);
+
+/* Conservation totals: sum over interior cells of (d, e, mx0, mx1, mx2),
+ * accumulated in FP64 on the device; waits for the stream. */
+int eulr_sim_totals(eulr_sim* sim, double out[5]);
+
+/* ------------------------------------------------------------ measurement */
+
+/* Times `iters` launches of a kernel whose warps issue only dependent-free
+ * FP64 FMAs (kind 0) or FP32 FMAs (kind 1) on all SMs; returns the achieved
+ * rate in FLOP/s (an FMA counts 2) via *flops.  Synchronous. */
+int eulr_probe_fma_rate(int kind, int iters, double* flops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EULER_GB300_H */

@@ -1,0 +1,37 @@
+/* CPU oracle for the Euler operators (TEST INFRASTRUCTURE ONLY).
+ *
+ * A plain-C restatement of the reference operator headers (euler_operators/), used by the
+ * tests, the smoke check and bench.py's CPU-baseline leg as the checker.  It is
+ * pinned bit-for-bit against the reference itself (oracle/_ref, built from the
+ * reference headers by oracle/Makefile) and against the golden fixtures under
+ * tests/golden/.  Build: see oracle/Makefile (-O2 -ffp-contract=off -fopenmp).
+ */
+#include <float.h>
+#include <math.h>
+#include <stddef.h>
+
+#include "euler_oracle.h"
+
+#define REAL double
+#define SUF f64
+#define SQRT sqrt
+#define FABS fabs
+#define REAL_MAX DBL_MAX
+#include "euler_oracle_body.h"
+#undef REAL
+#undef SUF
+#undef SQRT
+#undef FABS
+#undef REAL_MAX
+
+#define REAL float
+#define SUF f32
+#define SQRT sqrtf
+#define FABS fabsf
+#define REAL_MAX FLT_MAX
+#include "euler_oracle_body.h"
+#undef REAL
+#undef SUF
+#undef SQRT
+#undef FABS
+#undef REAL_MAX

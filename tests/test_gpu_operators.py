@@ -1,0 +1,148 @@
+"""GPU parity of the per-operator entry points against the oracle.
+
+prim_to_cons, cons_to_prim, time_step and init_implode are bit-identical to
+the reference (separately rounded arithmetic in the reference's order).
+godunov solves each face once and shares reciprocals, so it matches within
+the stated tolerance: 1e-12 relative L-infinity per field (max|a-b|/max|ref|)
+for FP64 after one call."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+TOL_F64_STEP = 1e-12
+TOL_F32_STEP = 2e-5  # float godunov: a few float ulps of the largest flux term
+
+OPS = sorted(glob.glob(os.path.join(GOLDEN, "ops_*.npz")))
+
+
+def _t(cuda, a):
+    return cuda.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("path", OPS, ids=os.path.basename)
+def test_golden_operators(cuda, euler, path):
+    z = np.load(path)
+    prim = z["prim"]
+    g = float(z["gamma"])
+    dx = tuple(float(v) for v in z["dx"])
+    cfl = float(z["cfl"])
+    pg = _t(cuda, prim)
+    cg = euler.prim_to_cons(pg, g)
+    assert np.array_equal(cg.cpu().numpy(), z["cons"])
+    assert np.array_equal(euler.cons_to_prim(cg, g).cpu().numpy(), z["prim_rt"])
+    dt = euler.time_step(pg, g, dx)
+    assert dt.item() == z["dt"][()]
+    euler.godunov(pg, cg, g, dx, cfl * z["dt"][()])
+    got = cg.cpu().numpy()
+    ref = z["cons_godunov"]
+    tol = TOL_F64_STEP if prim.dtype == np.float64 else TOL_F32_STEP
+    errs = rel_linf(got, ref)
+    assert max(errs) <= tol, errs
+    # ghosts are never touched
+    n2, n1, n0 = prim.shape[1:]
+    mask = np.ones((n2, n1, n0), bool)
+    if min(n0, n1, n2) >= 3:
+        mask[1:-1, 1:-1, 1:-1] = False
+    assert np.array_equal(got[:, mask], z["cons"][:, mask])
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_init_implode_bit_exact(cuda, euler, oracle_lib, dtype):
+    npdt = np.float64 if dtype == "f64" else np.float32
+    tdt = cuda.float64 if dtype == "f64" else cuda.float32
+    for n0, n1, n2 in ((18, 18, 18), (66, 34, 20), (7, 5, 3)):
+        dx = (1.0 / (n0 - 2), 1.0 / 17, 0.05)
+        ref = oracle_lib.init_implode(n0, n1, n2, dx, dtype=npdt)
+        got = euler.init_implode(n0, n1, n2, dx, dtype=tdt).cpu().numpy()
+        assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("shape", [(70, 40, 37), (34, 10, 130), (3, 3, 3), (5, 130, 4), (1, 1, 1), (2, 9, 9)])
+def test_random_operators_vs_oracle(cuda, euler, oracle_lib, shape):
+    O = oracle_lib
+    n0, n1, n2 = shape
+    prim = O.random_prim(n0, n1, n2, seed=sum(shape))
+    dx = (0.02, 0.03, 0.05)
+    g = 1.4
+    cons = O.prim_to_cons(prim, g)
+    dt = O.time_step(prim, g, dx)
+    ref = O.godunov(prim, cons, g, dx, 0.4 * dt)
+    pg = _t(cuda, prim)
+    cg = euler.prim_to_cons(pg, g)
+    assert np.array_equal(cg.cpu().numpy(), cons)
+    assert euler.time_step(pg, g, dx).item() == dt
+    euler.godunov(pg, cg, g, dx, 0.4 * dt)
+    errs = rel_linf(cg.cpu().numpy(), ref)
+    assert max(errs) <= TOL_F64_STEP, errs
+
+
+def test_godunov_device_dt_matches_host_dt(cuda, euler, oracle_lib):
+    O = oracle_lib
+    prim = O.random_prim(40, 33, 20, seed=4)
+    g, dx, cfl = 1.4, (0.1, 0.1, 0.1), 0.4
+    pg = _t(cuda, prim)
+    c1 = euler.prim_to_cons(pg, g)
+    c2 = c1.clone()
+    dt = euler.time_step(pg, g, dx)
+    euler.godunov(pg, c1, g, dx, (dt, cfl))
+    euler.godunov(pg, c2, g, dx, cfl * dt.item())
+    assert cuda.equal(c1, c2)
+
+
+def test_uniform_state_steady(cuda, euler):
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "uniform_*.npz"))):
+        z = np.load(path)
+        pg = _t(cuda, z["prim"])
+        cg = _t(cuda, z["cons"])
+        euler.godunov(pg, cg, float(z["gamma"]), tuple(float(v) for v in z["dx"]), float(z["dt_godunov"]))
+        assert np.array_equal(cg.cpu().numpy(), z["cons_godunov"])
+
+
+def test_time_step_edge_values(cuda, euler, oracle_lib):
+    """NaN cells are skipped, as the reference's Kokkos::min skips them."""
+    O = oracle_lib
+    prim = O.random_prim(9, 8, 7, seed=1)
+    prim[1, 3, 3, 3] = np.nan
+    dx = (0.1, 0.2, 0.3)
+    ref = O.time_step(prim, 1.4, dx)
+    got = euler.time_step(_t(cuda, prim), 1.4, dx).item()
+    assert got == ref
+
+
+def test_canary_guard_bands(cuda, euler, oracle_lib):
+    """Every kernel writes only inside its arrays: fields are carved out of
+    one buffer with canary gaps that must survive a full operator round."""
+    O = oracle_lib
+    n0, n1, n2 = 21, 13, 11
+    n = n0 * n1 * n2
+    gap = 64
+    prim = O.random_prim(n0, n1, n2, seed=8)
+    buf = cuda.full((10 * (n + gap) + gap,), 12345.0, dtype=cuda.float64, device="cuda")
+
+    def field(i):
+        off = gap + i * (n + gap)
+        return buf[off:off + n]
+
+    import euler_gb300 as E
+
+    pb = E.Bundle5(*[field(i).data_ptr() for i in range(5)])
+    cb = E.Bundle5(*[field(5 + i).data_ptr() for i in range(5)])
+    for i in range(5):
+        field(i).copy_(cuda.from_numpy(prim[i].ravel()))
+    lib = E.load()
+    s = cuda.cuda.current_stream().cuda_stream
+    import ctypes
+
+    E.check(lib.eulr_prim_to_cons_f64(pb, cb, n0, n1, n2, 1.4, ctypes.c_void_p(s)))
+    E.check(lib.eulr_godunov_f64(pb, cb, n0, n1, n2, 1.4, 0.1, 0.1, 0.1, 1e-3, ctypes.c_void_p(s)))
+    E.check(lib.eulr_cons_to_prim_f64(cb, pb, n0, n1, n2, 1.4, ctypes.c_void_p(s)))
+    cuda.cuda.synchronize()
+    for i in range(11):
+        off = i * (n + gap)
+        assert bool((buf[off:off + gap] == 12345.0).all()), f"canary {i} overwritten"

@@ -1,0 +1,138 @@
+"""GPU parity of the device-resident simulation (fused step) against the
+oracle's reference loop (time_step -> godunov(cfl*dt) -> cons_to_prim).
+
+Tolerances, relative L-infinity per field (max|a-b| / max|ref|):
+1e-12 after one step and 1e-10 after 100 steps, FP64."""
+import numpy as np
+import pytest
+
+from conftest import rel_linf
+
+pytestmark = pytest.mark.gpu
+
+TOL_1 = 1e-12
+TOL_100 = 1e-10
+
+
+def run_oracle_implode(O, nx, steps, cfl=0.4, gamma=1.4):
+    n = nx + 2
+    dx = (1.0 / nx,) * 3
+    prim = O.init_implode(n, n, n, dx)
+    cons = O.prim_to_cons(prim, gamma)
+    t = O.simulate(prim, cons, gamma, dx, cfl, steps)
+    return prim, cons, t
+
+
+@pytest.mark.parametrize("steps,tol", [(1, TOL_1), (2, TOL_1 * 4), (10, 1e-11), (100, TOL_100)])
+def test_implode_64(cuda, euler, oracle_lib, steps, tol):
+    nx = 64
+    prim_ref, cons_ref, t_ref = run_oracle_implode(oracle_lib, nx, steps)
+    n = nx + 2
+    with euler.Simulation(n, n, n, 1.4, (1.0 / nx,) * 3, 0.4) as sim:
+        sim.init_implode()
+        sim.advance(steps)
+        prim, cons = sim.state_numpy()
+        t, _, st = sim.time()
+        assert sim.status() == 0
+    assert st == steps
+    assert abs(t - t_ref) <= 1e-12 * t_ref
+    pe, ce = rel_linf(prim, prim_ref), rel_linf(cons, cons_ref)
+    assert max(pe) <= tol and max(ce) <= tol, (pe, ce)
+
+
+def test_implode_100_steps_time_and_totals(cuda, euler, oracle_lib):
+    """The 64^3 / 100-step configuration: simulated time and FP64
+    conservation totals against the oracle's."""
+    nx = 64
+    prim_ref, cons_ref, t_ref = run_oracle_implode(oracle_lib, nx, 100)
+    n = nx + 2
+    with euler.Simulation(n, n, n, 1.4, (1.0 / nx,) * 3, 0.4) as sim:
+        sim.init_implode()
+        tot0 = sim.totals()
+        sim.advance(100)
+        tot = sim.totals()
+        t, _, _ = sim.time()
+    assert abs(t - 0.121580552) < 1e-9
+    interior = cons_ref[:, 1:-1, 1:-1, 1:-1]
+    ref_tot = [float(interior[f].sum()) for f in range(5)]
+    for f in range(2):  # mass and energy: relative agreement
+        assert abs(tot[f] - ref_tot[f]) <= 1e-10 * abs(ref_tot[f])
+    for f in range(2, 5):  # momenta: start at 0, stay symmetric
+        assert abs(tot[f] - ref_tot[f]) <= 1e-10 * abs(tot0[0])
+
+
+def test_random_state_steps(cuda, euler, oracle_lib):
+    """Seeded random states (rho, p log-uniform [0.1,10], u ~ N(0,1)) on a
+    ragged grid: 1 and 5 steps."""
+    O = oracle_lib
+    n0, n1, n2 = 45, 38, 29
+    dx = (1 / 43, 1 / 36, 1 / 27)
+    prim0 = O.random_prim(n0, n1, n2, seed=21)
+    for steps, tol in ((1, TOL_1), (5, 1e-11)):
+        p = prim0.copy()
+        c = O.prim_to_cons(p, 1.4)
+        O.simulate(p, c, 1.4, dx, 0.4, steps)
+        with euler.Simulation(n0, n1, n2, 1.4, dx, 0.4) as sim:
+            sim.set_prim(prim0)
+            sim.advance(steps)
+            pg, cg = sim.state_numpy()
+        pe, ce = rel_linf(pg, p), rel_linf(cg, c)
+        assert max(pe) <= tol and max(ce) <= tol, (steps, pe, ce)
+
+
+def test_set_state_and_odd_step_counts(cuda, euler, oracle_lib):
+    """advance() in uneven chunks (graph replays plus single steps) equals
+    one long advance."""
+    O = oracle_lib
+    prim0 = O.random_prim(20, 24, 18, seed=2)
+    cons0 = O.prim_to_cons(prim0, 1.4)
+    dx = (0.05, 0.05, 0.05)
+    with euler.Simulation(20, 24, 18, 1.4, dx, 0.3) as a, euler.Simulation(20, 24, 18, 1.4, dx, 0.3) as b:
+        a.set_state(prim0, cons0)
+        b.set_state(prim0, cons0)
+        a.advance(7)
+        for k in (1, 3, 2, 1):
+            b.advance(k)
+        pa, ca = a.state_numpy()
+        pb, cb = b.state_numpy()
+    assert np.array_equal(pa, pb) and np.array_equal(ca, cb)
+
+
+def test_symmetry_of_implosion(cuda, euler):
+    """The implosion is symmetric under axis permutation: density stays
+    permutation-symmetric to rounding."""
+    nx = 32
+    n = nx + 2
+    with euler.Simulation(n, n, n, 1.4, (1.0 / nx,) * 3, 0.4) as sim:
+        sim.init_implode()
+        sim.advance(40)
+        prim, _ = sim.state_numpy()
+    d = prim[0]
+    scale = np.abs(d).max()
+    for perm in ((0, 2, 1), (1, 0, 2), (2, 1, 0)):
+        assert np.abs(d - d.transpose(perm)).max() <= 1e-12 * scale
+
+
+def test_tiny_and_degenerate_grids(cuda, euler, oracle_lib):
+    O = oracle_lib
+    for shape in ((3, 3, 3), (2, 5, 4), (35, 3, 3), (4, 4, 70)):
+        prim0 = O.random_prim(*shape, seed=7)
+        p = prim0.copy()
+        c = O.prim_to_cons(p, 1.4)
+        dx = (0.1, 0.1, 0.1)
+        O.simulate(p, c, 1.4, dx, 0.4, 3)
+        with euler.Simulation(*shape, 1.4, dx, 0.4) as sim:
+            sim.set_prim(prim0)
+            sim.advance(3)
+            pg, cg = sim.state_numpy()
+        assert max(rel_linf(pg, p)) <= 1e-11 and max(rel_linf(cg, c)) <= 1e-11, shape
+
+
+def test_nonphysical_state_is_reported(cuda, euler, oracle_lib):
+    """A host-injected negative pressure is flagged, not trapped."""
+    prim0 = oracle_lib.random_prim(16, 16, 16, seed=3)
+    prim0[1, 8, 8, 8] = -5.0
+    with euler.Simulation(16, 16, 16, 1.4, (0.1,) * 3, 0.4) as sim:
+        sim.set_prim(prim0)
+        sim.advance(2)
+        assert sim.status() == -7  # EULR_ERR_NONFINITE

@@ -1,0 +1,102 @@
+"""CPU tests of the oracle: the C restatement against the golden fixtures
+generated by the reference itself (tests/golden/make_golden.py), and against
+the reference build where it exists.  Bit-exact: the oracle keeps the
+reference's operand order and is compiled with -ffp-contract=off."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+OPS = sorted(glob.glob(os.path.join(GOLDEN, "ops_*.npz")))
+IMPLODE = sorted(glob.glob(os.path.join(GOLDEN, "implode_*.npz")))
+UNIFORM = sorted(glob.glob(os.path.join(GOLDEN, "uniform_*.npz")))
+
+
+def test_fixtures_present():
+    assert len(OPS) == 8 and len(IMPLODE) == 2 and len(UNIFORM) == 2
+
+
+@pytest.mark.parametrize("path", OPS, ids=os.path.basename)
+def test_operators_bit_exact(oracle_lib, path):
+    O = oracle_lib
+    z = np.load(path)
+    prim = z["prim"]
+    g = float(z["gamma"])
+    dx = tuple(float(v) for v in z["dx"])
+    cons = O.prim_to_cons(prim, g)
+    assert np.array_equal(cons, z["cons"])
+    assert np.array_equal(O.cons_to_prim(cons, g), z["prim_rt"])
+    dt = O.time_step(prim, g, dx)
+    assert dt == z["dt"][()]
+    out = O.godunov(prim, cons, g, dx, float(z["cfl"]) * dt)
+    assert np.array_equal(out, z["cons_godunov"])
+
+
+@pytest.mark.parametrize("path", UNIFORM, ids=os.path.basename)
+def test_uniform_state_is_steady(oracle_lib, path):
+    O = oracle_lib
+    z = np.load(path)
+    g = float(z["gamma"])
+    dx = tuple(float(v) for v in z["dx"])
+    cons = O.prim_to_cons(z["prim"], g)
+    assert np.array_equal(cons, z["cons"])
+    assert O.time_step(z["prim"], g, dx) == z["dt"][()]
+    out = O.godunov(z["prim"], cons, g, dx, float(z["dt_godunov"]))
+    assert np.array_equal(out, z["cons_godunov"])
+    assert np.array_equal(out, cons)  # a uniform state has zero net flux
+
+
+@pytest.mark.parametrize("path", IMPLODE, ids=os.path.basename)
+def test_implode_bit_exact(oracle_lib, path):
+    O = oracle_lib
+    z = np.load(path)
+    g, cfl = float(z["gamma"]), float(z["cfl"])
+    dx = tuple(float(v) for v in z["dx"])
+    n = z["prim0"].shape[1]
+    prim = O.init_implode(n, n, n, dx, dtype=z["prim0"].dtype)
+    assert np.array_equal(prim, z["prim0"])
+    cons = O.prim_to_cons(prim, g)
+    assert np.array_equal(cons, z["cons0"])
+    t = 0.0
+    done = 0
+    for s in (1, 10):
+        t += O.simulate(prim, cons, g, dx, cfl, s - done)
+        done = s
+        assert np.array_equal(prim, z[f"prim_{s}"])
+        assert np.array_equal(cons, z[f"cons_{s}"])
+        assert t == z[f"t_{s}"][()]
+
+
+def test_port_matches_reference_build(oracle_lib):
+    """Where the reference checkout exists, the port agrees with it bit for
+    bit on fresh seeded inputs too."""
+    O = oracle_lib
+    if not os.path.isdir(os.path.join(O.REFERENCE_DIR, "euler_operators")):
+        pytest.skip("reference checkout not present")
+    O.build(ref=True)
+    for dtype in (np.float64, np.float32):
+        for shape in ((11, 6, 9), (4, 4, 4)):
+            prim = O.random_prim(*shape, seed=99, dtype=dtype)
+            dx = (0.3, 0.2, 0.1)
+            for impl_a, impl_b in (("port", "ref"),):
+                ca, cb = O.prim_to_cons(prim, 1.3, impl=impl_a), O.prim_to_cons(prim, 1.3, impl=impl_b)
+                assert np.array_equal(ca, cb)
+                assert O.time_step(prim, 1.3, dx, impl=impl_a) == O.time_step(prim, 1.3, dx, impl=impl_b)
+                assert np.array_equal(O.godunov(prim, ca, 1.3, dx, 1e-3, impl=impl_a),
+                                      O.godunov(prim, cb, 1.3, dx, 1e-3, impl=impl_b))
+                assert np.array_equal(O.cons_to_prim(ca, 1.3, impl=impl_a), O.cons_to_prim(cb, 1.3, impl=impl_b))
+
+
+def test_implode_64_reference_time(oracle_lib):
+    """64^3 implosion, 100 steps at CFL 0.4: the simulated time the reference
+    build reaches (0.121580552 to 9 digits)."""
+    O = oracle_lib
+    nx = 64
+    dx = (1.0 / nx,) * 3
+    prim = O.init_implode(nx + 2, nx + 2, nx + 2, dx)
+    cons = O.prim_to_cons(prim, 1.4)
+    t = O.simulate(prim, cons, 1.4, dx, 0.4, 100)
+    assert abs(t - 0.121580552) < 5e-10
