@@ -55,6 +55,7 @@ _SIGNATURES = [
     ("eulr_cons_to_prim_f32", _I, [Bundle5, Bundle5, _I, _I, _I, _F, _P]),
     ("eulr_time_step_f64", _I, [Bundle5, _I, _I, _I, _D, _D, _D, _D, _P, _P]),
     ("eulr_time_step_f32", _I, [Bundle5, _I, _I, _I, _F, _F, _F, _F, _P, _P]),
+    ("eulr_time_step_noalloc_f64", _I, [Bundle5, _I, _I, _I, _D, _D, _D, _D, _P, _P]),
     ("eulr_godunov_f64", _I, [Bundle5, Bundle5, _I, _I, _I, _D, _D, _D, _D, _D, _P]),
     ("eulr_godunov_f32", _I, [Bundle5, Bundle5, _I, _I, _I, _F, _F, _F, _F, _F, _P]),
     ("eulr_godunov_devdt_f64", _I, [Bundle5, Bundle5, _I, _I, _I, _D, _D, _D, _D, _P, _D, _P]),

@@ -161,6 +161,23 @@ int eulr_time_step_f64(eulr_prim_cf64 prim, int n0, int n1, int n2, double gamma
 int eulr_time_step_f32(eulr_prim_cf32 prim, int n0, int n1, int n2, float gamma, float dx0, float dx1,
                        float dx2, float* dt_out, eulr_stream_t stream);
 
+/* eulr_time_step_f64 for callers that cannot allocate device memory -- code
+ * whose device memory is owned by a pool or arena that forbids hidden
+ * allocations, or that must know the library's full device footprint up
+ * front.  No counterpart in the reference (its time_step allocates nothing
+ * itself because Kokkos manages the reduction).  Same arguments and same
+ * bit-identical result as eulr_time_step_f64; it calls no cudaMalloc/cudaFree
+ * and no allocating routine.  Its scratch is a fixed ~8 KiB array inside the
+ * library's device image (1024 block maxima and a counter), held by every
+ * GPU that loads the library until exit; every grid below 2^31 cells fits,
+ * larger ones return EULR_ERR_TOO_LARGE.  The first call on each device
+ * looks up the array's address (cudaGetSymbolAddress) and should come before
+ * any stream capture on that device.  All calls on a device share the array:
+ * calls whose kernels can overlap on the GPU (e.g. unordered streams) race
+ * and must not be issued. */
+int eulr_time_step_noalloc_f64(eulr_prim_cf64 prim, int n0, int n1, int n2, double gamma, double dx0, double dx1,
+                               double dx2, double* dt_out, eulr_stream_t stream);
+
 /* godunov (euler_operators/godunov.hpp:15-92): for interior cells,
  * cons -= dt/dv * sum_d ds_d (F_{d,R} - F_{d,L}) with HLLC fluxes
  * (euler_operators/hllc.hpp:50-105) from the read-only prim; cons is updated
