@@ -310,8 +310,12 @@ def run_ours(args):
     # roofline of the fused kernel on the FP64 pipe
     fpc = flops_per_cell()
     peak = E.fma_rate("f64")
+    props = torch.cuda.get_device_properties(local)
+    nominal = 2 * 2 * props.multi_processor_count * 2.07e9  # 2 DFMA/clk/SM at the 2070 MHz max clock
     roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak / 1e12,
-            "peak_source": "measured in this run: FP64 FMA probe (eulr_probe_fma_rate), FMA = 2 FLOP",
+            "peak_source": "measured in this run: FP64 FMA probe (eulr_probe_fma_rate), FMA = 2 FLOP; "
+                           "the probe itself runs the FP64 pipe at ~84% of ncu's nominal 2 DFMA/clk/SM",
+            "peak_nominal": nominal / 1e12,
             "kernel": "flux_tile_kernel<double, step>", "kernel_ms": flux_ms,
             "step_ms_sum_of_launches": step_ms_launches, "traffic": None}
     if fpc:

@@ -307,6 +307,7 @@ int godunov_impl(PB prim, CB cons, int n0, int n1, int n2, T gamma, T dx0, T dx1
     p.gamma = gamma;
     p.gm1 = gamma - T(1);
     p.inv_gm1 = T(1) / (gamma - T(1));
+    p.half_gm1 = T(0.5) * (gamma - T(1));
     p.ds0 = dx1 * dx2; // uniform_mesh.hpp:62-75
     p.ds1 = dx2 * dx0;
     p.ds2 = dx0 * dx1;
@@ -314,8 +315,8 @@ int godunov_impl(PB prim, CB cons, int n0, int n1, int n2, T gamma, T dx0, T dx1
     p.dtodv = dt / p.dv;
     p.dt_dev = dt_dev;
     p.cfl = cfl;
-    EULR_CUDA_TRY(configure_flux<T>(kModeGodunov, &p.per_sm), "godunov configure");
-    EULR_CUDA_TRY(launch_flux<T>(p, kModeGodunov, sms, s), "godunov launch");
+    EULR_CUDA_TRY(configure_flux<T>(kModeGodunov, false, &p.per_sm), "godunov configure");
+    EULR_CUDA_TRY(launch_flux<T>(p, nullptr, kModeGodunov, sms, s), "godunov launch");
     return EULR_SUCCESS;
 }
 

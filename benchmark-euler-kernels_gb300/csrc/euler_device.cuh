@@ -144,48 +144,137 @@ struct Flux {
     T d, e, n, t1, t2;
 };
 
-// HLLC flux of hllc::operator() (euler_operators/hllc.hpp:50-105) in the face
-// frame.  Wave speeds (:64-68), acoustic star state (:70-76), upwind side by
-// the sign of ustar (:78-79), supersonic test S_L*S_R > 0 (:84-85), star
-// density and energy (:86-88) and the flux (:90-102).  The two divisions by
-// (S - un_o) and (S - ustar) of the reference share one reciprocal: they have
-// the same denominator in the subsonic case, and in the supersonic case the
-// reference's ratio (S-un)/(S-un) is exactly 1 and its energy correction is
-// exactly 0, which is what the select below produces.
-template <class T>
-__device__ __forceinline__ Flux<T> hllc_flux(Side<T> const& L, Side<T> const& R)
+// ------------------------------------------------- integer-pipe predicates
+// On GB300 an FP64 compare, min or max takes a full slot of the FP64 pipe
+// (1/64 of the FP32 rate); the same decisions taken on the bit patterns run
+// on the integer pipe, which the flux kernels leave almost idle.
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+// Signed key with the order of the doubles (-0 sorts just below +0).
+__device__ __forceinline__ long long order_key(double x)
 {
-    T const cmax = fmax(L.c, R.c);
-    T const S_L = fmin(L.un, R.un) - cmax;
-    T const S_R = fmax(L.un, R.un) + cmax;
+    long long const b = dbits(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
 
-    T const rc_L = L.d * (S_L - L.un);
-    T const rc_R = R.d * (S_R - R.un);
+// x is neither +0 nor -0.
+__device__ __forceinline__ bool nonzero_(double x) { return (dbits(x) << 1) != 0; }
 
-    T const ustar = (R.p - L.p + rc_L * L.un - rc_R * R.un) / (rc_L - rc_R);
-    T const pstar = T(0.5) * (L.p + R.p + rc_L * (ustar - L.un) + rc_R * (ustar - R.un));
+// a*b > 0 for non-NaN a, b, decided from signs: both non-zero and of one sign.
+__device__ __forceinline__ bool product_positive(double a, double b)
+{
+    return nonzero_(a) && nonzero_(b) && ((dbits(a) ^ dbits(b)) >= 0);
+}
 
-    bool const left = ustar > T(0);
-    T const S = left ? S_L : S_R;
-    T const qd = left ? L.d : R.d;
-    T const qp = left ? L.p : R.p;
-    T const qun = left ? L.un : R.un;
-    T const qut1 = left ? L.ut1 : R.ut1;
-    T const qut2 = left ? L.ut2 : R.ut2;
-    T const qe = left ? L.e : R.e;
+// Finite and > 0.
+__device__ __forceinline__ bool finite_positive(double x)
+{
+    long long const b = dbits(x);
+    return b > 0 && b < 0x7ff0000000000000LL;
+}
 
-    bool const supersonic = S_L * S_R > T(0);
-    T const inv = T(1) / (S - ustar);
-    T const ratio = (S - qun) * inv;
-    T const d_star = ratio * qd;
-    T const e_star = ratio * qe + (pstar * ustar - qp * qun) * inv;
+// HLLC flux of hllc::operator() (euler_operators/hllc.hpp:50-105) in the face
+// frame: wave speeds (:64-68), acoustic star state (:70-76), upwind side by
+// the sign of ustar (:78-79), supersonic test S_L*S_R > 0 (:84-85), star
+// density and energy (:86-88) and the flux (:90-102).  Reformulated to spend
+// as few FP64 instructions as possible; in exact arithmetic it is the same
+// function:
+//  * ustar = num/den and 1/(S - ustar) = den/(S den - num) come from ONE
+//    reciprocal R = 1/(den (S den - num)): ustar = num (S den - num) R and
+//    1/(S - ustar) = den^2 R.  The side (sign of ustar) is read from the signs
+//    of num and den before any division.
+//  * pstar: the reference averages p_L + rc_L (ustar-u_L) and
+//    p_R + rc_R (ustar-u_R), which are equal by the definition of ustar; the
+//    upwind one is used.  The star energy term (pstar ustar - p un) then
+//    factors as (ustar - un)(p + rc ustar), which has no cancellation.
+//  * in the supersonic case the reference's ratio (S-un)/(S-un) is exactly 1
+//    and its energy correction exactly 0: a select returns the upwind state.
+//  * min/max and the sign tests run on the integer pipe (order_key etc.).
+// Results agree with the reference to a few ulps per face.
+__device__ __forceinline__ Flux<double> hllc_flux(Side<double> const& L, Side<double> const& R)
+{
+    double const cmax = (dbits(L.c) > dbits(R.c)) ? L.c : R.c; // sound speeds are >= 0
+    bool const lt = order_key(L.un) < order_key(R.un);
+    double const umin = lt ? L.un : R.un;
+    double const umax = lt ? R.un : L.un;
+    double const S_L = umin - cmax;
+    double const S_R = umax + cmax;
 
-    T const un_o = supersonic ? qun : ustar;
-    T const ptot_o = supersonic ? qp : pstar;
-    T const d_o = supersonic ? qd : d_star;
-    T const e_o = supersonic ? qe : e_star;
+    double const rc_L = L.d * (S_L - L.un);
+    double const rc_R = R.d * (S_R - R.un);
+    double const num = (R.p - L.p) + rc_L * L.un - rc_R * R.un;
+    double const den = rc_L - rc_R;
 
-    Flux<T> f;
+    bool const left = product_positive(num, den); // ustar > 0
+    double const S = left ? S_L : S_R;
+    double const qd = left ? L.d : R.d;
+    double const qp = left ? L.p : R.p;
+    double const qun = left ? L.un : R.un;
+    double const qut1 = left ? L.ut1 : R.ut1;
+    double const qut2 = left ? L.ut2 : R.ut2;
+    double const qe = left ? L.e : R.e;
+    double const qrc = left ? rc_L : rc_R;
+
+    double const M = S * den - num; // den (S - ustar)
+    double const Rr = __drcp_rn(den * M);
+    double const ustar = num * (M * Rr);
+    double const inv = den * (den * Rr); // 1 / (S - ustar)
+    double const w = ustar - qun;
+    double const pstar = qp + qrc * w;
+
+    bool const supersonic = product_positive(S_L, S_R);
+    double const ratio = (S - qun) * inv;
+    double const d_star = ratio * qd;
+    double const e_star = ratio * qe + w * (qp + qrc * ustar) * inv;
+
+    double const un_o = supersonic ? qun : ustar;
+    double const ptot_o = supersonic ? qp : pstar;
+    double const d_o = supersonic ? qd : d_star;
+    double const e_o = supersonic ? qe : e_star;
+
+    Flux<double> f;
+    f.d = d_o * un_o;
+    f.e = (e_o + ptot_o) * un_o;
+    f.n = f.d * un_o + ptot_o;
+    f.t1 = f.d * qut1;
+    f.t2 = f.d * qut2;
+    return f;
+}
+
+// FP32 version (real_t = float operators): same algebra, FP32 min/max.
+__device__ __forceinline__ Flux<float> hllc_flux(Side<float> const& L, Side<float> const& R)
+{
+    float const cmax = fmaxf(L.c, R.c);
+    float const S_L = fminf(L.un, R.un) - cmax;
+    float const S_R = fmaxf(L.un, R.un) + cmax;
+    float const rc_L = L.d * (S_L - L.un);
+    float const rc_R = R.d * (S_R - R.un);
+    float const num = (R.p - L.p) + rc_L * L.un - rc_R * R.un;
+    float const den = rc_L - rc_R;
+    bool const left = (num > 0.0f) == (den > 0.0f) && num != 0.0f && den != 0.0f;
+    float const S = left ? S_L : S_R;
+    float const qd = left ? L.d : R.d;
+    float const qp = left ? L.p : R.p;
+    float const qun = left ? L.un : R.un;
+    float const qut1 = left ? L.ut1 : R.ut1;
+    float const qut2 = left ? L.ut2 : R.ut2;
+    float const qe = left ? L.e : R.e;
+    float const qrc = left ? rc_L : rc_R;
+    float const M = S * den - num;
+    float const Rr = __frcp_rn(den * M);
+    float const ustar = num * (M * Rr);
+    float const inv = den * (den * Rr);
+    float const w = ustar - qun;
+    float const pstar = qp + qrc * w;
+    bool const supersonic = S_L * S_R > 0.0f;
+    float const ratio = (S - qun) * inv;
+    float const d_star = ratio * qd;
+    float const e_star = ratio * qe + w * (qp + qrc * ustar) * inv;
+    float const un_o = supersonic ? qun : ustar;
+    float const ptot_o = supersonic ? qp : pstar;
+    float const d_o = supersonic ? qd : d_star;
+    float const e_o = supersonic ? qe : e_star;
+    Flux<float> f;
     f.d = d_o * un_o;
     f.e = (e_o + ptot_o) * un_o;
     f.n = f.d * un_o + ptot_o;

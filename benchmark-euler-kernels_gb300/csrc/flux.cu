@@ -4,21 +4,30 @@
 // Work decomposition: the interior [1,n0-1) x [1,n1-1) x [1,n2-1) is cut into
 // TX x TY columns and each column into chunks of kchunk planes; a persistent
 // grid of CTAs walks the (tile, chunk) items round-robin.  A CTA marches up
-// its chunk one plane at a time with a ring of plane slots in shared memory,
-// each slot holding the 7 face inputs (d, p, u0, u1, u2, c, e) of a
+// its chunk one plane at a time through a ring of plane slots in shared
+// memory, each slot holding the 7 face inputs (d, p, u0, u1, u2, c, e) of a
 // (TX+2) x (TY+2) plane with its one-cell halo.  Per plane:
 //   1. face phase -- every x face and y face of plane k and every z face
 //      between planes k and k+1 is solved ONCE (the reference solves each
 //      interior face twice, once from each side, godunov.hpp:48-82); the
-//      808 faces of a 32x8 tile are spread linearly over the 256 threads,
-//      97% lane occupancy, and fluxes go to shared memory in global axes;
-//   2. cell phase -- each thread owns one column cell, sums
-//      ds_d (F_R - F_L) over the three axes in the reference's order and
-//      applies cons -= dt/dv * flux (godunov.hpp:84-90).  The z face below
-//      the cell is carried in registers from the previous plane.
+//      808 faces of a 32x8 tile are spread linearly over the 256 threads
+//      (97% lane occupancy) and fluxes go to shared memory in global axes;
+//   2. cell phase -- each thread owns one column cell and applies
+//      cons -= dt/dv * sum_d ds_d (F_R - F_L) (godunov.hpp:84-90) with the
+//      face-area and dt/dv factors folded into three coefficients.  The z
+//      face below the cell is carried in registers from the previous plane.
 // The fused step then finishes the cell on chip: cons_to_prim, sound speed
 // and the next step's CFL max-wavespeed, reduced warp -> block -> one
 // atomicMax per CTA, so dt never leaves the device.
+//
+// Staging: in the fused step the seven input fields of a plane slot are
+// fetched by TMA (cp.async.bulk.tensor, one 34x10x1 box per field) into a
+// ring of three slots, two planes ahead of the plane being solved, each slot
+// completing on its own mbarrier.  Grids whose row pitch is not a multiple of
+// 16 bytes (odd n0) and the per-operator godunov (arbitrary caller pointers)
+// stage with plain cooperative loads instead.  Every mbarrier wait is bounded:
+// a wait that runs out sets bit 1 of the status word, waits (bounded) for the
+// copies still in flight and ends the CTA.
 #include "euler_device.cuh"
 #include "kernels.h"
 
@@ -28,38 +37,104 @@ namespace eulr {
 
 namespace {
 
-constexpr int kFields = 7; // d, p, u0, u1, u2, c, e
+constexpr int kFields = 7;          // d, p, u0, u1, u2, c, e
+constexpr int kWaitTries = 1 << 20; // mbarrier.try_wait attempts before giving up
+constexpr long long kInfBits = 0x7ff0000000000000LL;
 
 template <class T, int TX, int TY, int NSLOT>
 struct TileLayout {
     static constexpr int HX = TX + 2;
     static constexpr int HY = TY + 2;
     static constexpr int PLANE = HX * HY;
+    static constexpr int PLANE_PAD = (PLANE + 15) / 16 * 16; // 128-byte aligned field tiles
     static constexpr int NFX = (TX + 1) * TY;
     static constexpr int NFY = TX * (TY + 1);
     static constexpr int NFZ = TX * TY;
     static constexpr int NFACE = NFX + NFY + NFZ;
     static constexpr int NT = TX * TY;
-    // shared memory in T elements
-    static constexpr int Q_ELEMS = NSLOT * kFields * PLANE;
+    // shared memory, in T elements after a 128-byte mbarrier block
+    static constexpr int Q_ELEMS = NSLOT * kFields * PLANE_PAD;
     static constexpr int FX_OFF = Q_ELEMS;
     static constexpr int FY_OFF = FX_OFF + 5 * NFX;
     static constexpr int FZ_OFF = FY_OFF + 5 * NFY;
     static constexpr int ELEMS = FZ_OFF + 5 * NFZ;
-    static constexpr size_t BYTES = sizeof(T) * static_cast<size_t>(ELEMS);
+    static constexpr int MBAR_BYTES = 128;
+    // + 128 bytes of slack to align the dynamic region to 128 bytes at run time
+    static constexpr size_t BYTES = 128 + MBAR_BYTES + sizeof(T) * static_cast<size_t>(ELEMS);
+    static constexpr unsigned TX_BYTES = kFields * PLANE * sizeof(T); // bytes one slot's TMA delivers
 };
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false if it never came.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity)
+{
+    unsigned const a = smem_u32(bar);
+    for (int it = 0; it < kWaitTries; ++it) {
+        unsigned done;
+        asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(done)
+                : "r"(a), "r"(parity)
+                : "memory");
+        if (done) {
+            return true;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar)
+{
+    asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+            "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+            : "memory");
+}
 
 template <class T, int TX, int TY, int NSLOT>
 __device__ __forceinline__ T* slot_field(T* smem, int slot, int field)
 {
     using L = TileLayout<T, TX, TY, NSLOT>;
-    return smem + (slot * kFields + field) * L::PLANE;
+    return smem + (slot * kFields + field) * L::PLANE_PAD;
 }
 
-// Stage plane k of the tile whose first interior cell is (i0, j0) into `slot`.
-// Godunov mode derives c and e from prim; step mode reads the stored sound
-// speed and the conservative energy.  Cells outside the array get a benign
-// uniform state; no face touching them is ever used.
+// Issue the TMA loads of plane k (x origin i0-1, y origin j0-1) into `slot`.
+template <class T, int TX, int TY, int NSLOT>
+__device__ __forceinline__ void issue_plane(T* smem, unsigned long long* bars, int slot, TmaMaps const& maps, int i0,
+                                            int j0, int k)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bars[slot], L::TX_BYTES);
+#pragma unroll
+    for (int f = 0; f < kFields; ++f) {
+        tma_load_3d(slot_field<T, TX, TY, NSLOT>(smem, slot, f), &maps.m[f], i0 - 1, j0 - 1, k, &bars[slot]);
+    }
+}
+
+// Stage plane k with plain loads.  Godunov mode derives c and e from prim;
+// step mode reads the stored sound speed and the conservative energy.  Cells
+// outside the array get a benign uniform state; no face touching them is
+// ever used.
 template <class T, int TX, int TY, int NSLOT, int MODE>
 __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> const& p, int i0, int j0, int k)
 {
@@ -87,27 +162,27 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
                 e = pr * p.inv_gm1 + T(0.5) * d * (u0 * u0 + u1 * u1 + u2 * u2);
             }
         }
-        q[0 * L::PLANE + c] = d;
-        q[1 * L::PLANE + c] = pr;
-        q[2 * L::PLANE + c] = u0;
-        q[3 * L::PLANE + c] = u1;
-        q[4 * L::PLANE + c] = u2;
-        q[5 * L::PLANE + c] = cs;
-        q[6 * L::PLANE + c] = e;
+        q[0 * L::PLANE_PAD + c] = d;
+        q[1 * L::PLANE_PAD + c] = pr;
+        q[2 * L::PLANE_PAD + c] = u0;
+        q[3 * L::PLANE_PAD + c] = u1;
+        q[4 * L::PLANE_PAD + c] = u2;
+        q[5 * L::PLANE_PAD + c] = cs;
+        q[6 * L::PLANE_PAD + c] = e;
     }
 }
 
-template <class T, int PLANE>
+template <class T, int PLANE_PAD>
 __device__ __forceinline__ Side<T> load_side(T const* q, int c, int dir)
 {
     Side<T> s;
-    s.d = q[0 * PLANE + c];
-    s.p = q[1 * PLANE + c];
-    s.un = q[(2 + dir) * PLANE + c];
-    s.ut1 = q[(2 + (dir + 1) % 3) * PLANE + c];
-    s.ut2 = q[(2 + (dir + 2) % 3) * PLANE + c];
-    s.c = q[5 * PLANE + c];
-    s.e = q[6 * PLANE + c];
+    s.d = q[0 * PLANE_PAD + c];
+    s.p = q[1 * PLANE_PAD + c];
+    s.un = q[(2 + dir) * PLANE_PAD + c];
+    s.ut1 = q[(2 + (dir + 1) % 3) * PLANE_PAD + c];
+    s.ut2 = q[(2 + (dir + 2) % 3) * PLANE_PAD + c];
+    s.c = q[5 * PLANE_PAD + c];
+    s.e = q[6 * PLANE_PAD + c];
     return s;
 }
 
@@ -121,12 +196,38 @@ __device__ __forceinline__ void store_flux(T* out, int stride, int idx, int dir,
     out[(2 + (dir + 2) % 3) * stride + idx] = f.t2;
 }
 
-template <class T, int TX, int TY, int NSLOT, int MODE>
-__global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
+// Sound speed sqrt(gamma p / rho) = x * rsqrt(x): rsqrt costs fewer FP64
+// instructions than a correctly rounded sqrt; the result is within ~2 ulps.
+__device__ __forceinline__ double fast_sound_speed(double c2) { return c2 * rsqrt(c2); }
+__device__ __forceinline__ float fast_sound_speed(float c2) { return c2 * rsqrtf(c2); }
+
+__device__ __forceinline__ long long wave_key(double v)
+{
+    long long const b = dbits(v);
+    return b <= kInfBits ? b : 0LL; // NaN never wins (the reference skips it)
+}
+__device__ __forceinline__ long long wave_key(float v) { return wave_key(static_cast<double>(v)); }
+
+__device__ __forceinline__ bool cell_ok(double d, double pr, double invdt)
+{
+    return finite_positive(d) && finite_positive(pr) && dbits(invdt) < kInfBits;
+}
+__device__ __forceinline__ bool cell_ok(float d, float pr, float invdt)
+{
+    return d > 0.0f && pr > 0.0f && invdt <= 3.0e38f;
+}
+
+template <class T, int TX, int TY, int NSLOT, int MODE, bool TMA>
+__global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant__ FluxParams<T> p,
+                                                           const __grid_constant__ TmaMaps maps)
 {
     using L = TileLayout<T, TX, TY, NSLOT>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* smem = reinterpret_cast<T*>(smem_raw);
+    static_assert(!TMA || NSLOT == 3, "the TMA ring has three slots");
+    extern __shared__ __align__(128) unsigned char smem_dyn[];
+    // TMA destinations must sit on 128-byte boundaries of the shared window
+    unsigned char* smem_raw = smem_dyn + ((128u - (smem_u32(smem_dyn) & 127u)) & 127u);
+    auto* bars = reinterpret_cast<unsigned long long*>(smem_raw);
+    T* smem = reinterpret_cast<T*>(smem_raw + L::MBAR_BYTES);
     T* fx = smem + L::FX_OFF;
     T* fy = smem + L::FY_OFF;
     T* fz = smem + L::FZ_OFF;
@@ -136,15 +237,36 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
         T const dtc = p.cfl * *p.dt_dev; // cfl * dt, euler_simulation.cpp:65
         dtodv = dtc / p.dv;              // godunov.hpp:37
     }
-    T const ds0 = p.ds0, ds1 = p.ds1, ds2 = p.ds2;
+    // cons -= dt/dv * sum_d ds_d (F_R - F_L), coefficients folded
+    T const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2;
 
     int const tid = threadIdx.x;
     int const ti = tid % TX;
     int const tj = tid / TX;
     int const center = (tj + 1) * L::HX + ti + 1;
 
-    T wmax = T(0);
+    long long wkey = 0;
     bool bad = false;
+    unsigned phase = 0;    // bit s: parity of slot s's next completion (TMA ring)
+    unsigned inflight = 0; // bit s: a TMA into slot s has not been waited for
+    bool timed_out = false;
+
+    if (TMA) {
+        if (tid == 0) {
+            for (int s = 0; s < NSLOT; ++s) {
+                mbar_init(&bars[s], 1);
+            }
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+    }
+
+    auto wait_slot = [&](int s) -> bool {
+        bool const ok = mbar_wait(&bars[s], (phase >> s) & 1u);
+        phase ^= 1u << s;
+        inflight &= ~(1u << s);
+        return ok;
+    };
 
     int const tiles_xy = p.tiles_x * p.tiles_y;
     for (int w = blockIdx.x; w < p.nwork; w += gridDim.x) {
@@ -159,28 +281,51 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
         int const j = j0 + tj;
         bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
 
-        __syncthreads(); // previous item's readers of the slots are done
-        load_plane<T, TX, TY, NSLOT, MODE>(smem, 0, p, i0, j0, kb - 1);
-        load_plane<T, TX, TY, NSLOT, MODE>(smem, 1, p, i0, j0, kb);
-        __syncthreads();
+        __syncthreads(); // the previous item's readers of slots and fluxes are done
+        if (TMA) {
+            // planes kb-1, kb, kb+1 -> slots 0, 1, 2 (kb+1 <= ke always)
+            if (tid == 0) {
+                issue_plane<T, TX, TY, NSLOT>(smem, bars, 0, maps, i0, j0, kb - 1);
+                issue_plane<T, TX, TY, NSLOT>(smem, bars, 1, maps, i0, j0, kb);
+                issue_plane<T, TX, TY, NSLOT>(smem, bars, 2, maps, i0, j0, kb + 1);
+            }
+            inflight |= 7u;
+            timed_out |= !wait_slot(0);
+            timed_out |= !wait_slot(1);
+        } else {
+            load_plane<T, TX, TY, NSLOT, MODE>(smem, 0, p, i0, j0, kb - 1);
+            load_plane<T, TX, TY, NSLOT, MODE>(smem, 1, p, i0, j0, kb);
+            __syncthreads();
+        }
         // z face below the chunk's first plane, kept in registers in global
         // axes (the z face frame has n = mx2, t1 = mx0, t2 = mx1)
         T zlo[5];
         {
-            Flux<T> const f0 = hllc_flux(load_side<T, L::PLANE>(slot_field<T, TX, TY, NSLOT>(smem, 0, 0), center, 2),
-                                         load_side<T, L::PLANE>(slot_field<T, TX, TY, NSLOT>(smem, 1, 0), center, 2));
+            Flux<T> const f0 =
+                    hllc_flux(load_side<T, L::PLANE_PAD>(slot_field<T, TX, TY, NSLOT>(smem, 0, 0), center, 2),
+                              load_side<T, L::PLANE_PAD>(slot_field<T, TX, TY, NSLOT>(smem, 1, 0), center, 2));
             zlo[0] = f0.d;
             zlo[1] = f0.e;
             zlo[2] = f0.t1;
             zlo[3] = f0.t2;
             zlo[4] = f0.n;
         }
-        __syncthreads(); // slot 0 is refilled by the first plane of the loop
+        if (__syncthreads_or(timed_out)) { // slot 0 is refilled next
+            break;
+        }
+        if (TMA) {
+            if (kb + 2 <= ke) {
+                if (tid == 0) {
+                    issue_plane<T, TX, TY, NSLOT>(smem, bars, 0, maps, i0, j0, kb + 2);
+                }
+                inflight |= 1u;
+            }
+        }
 
         for (int k = kb; k < ke; ++k) {
             int const cur = (k - kb + 1) % NSLOT;
             int const nxt = (k - kb + 2) % NSLOT;
-            // prefetch this cell's conservative state
+            // this cell's conservative state, fetched while the faces are solved
             T u[5];
             long long const o = p.g.at(i, j, k);
             if (own) {
@@ -189,8 +334,12 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
                     u[f] = p.cons_in.f[f][o];
                 }
             }
-            load_plane<T, TX, TY, NSLOT, MODE>(smem, nxt, p, i0, j0, k + 1);
-            __syncthreads();
+            if (TMA) {
+                timed_out |= !wait_slot(nxt);
+            } else {
+                load_plane<T, TX, TY, NSLOT, MODE>(smem, nxt, p, i0, j0, k + 1);
+                __syncthreads();
+            }
 
             // ---- face phase
             T const* qc = slot_field<T, TX, TY, NSLOT>(smem, cur, 0);
@@ -201,32 +350,43 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
                     int const fi = f % (TX + 1);
                     int const a = (fj + 1) * L::HX + fi;
                     store_flux(fx, L::NFX, f, 0,
-                               hllc_flux(load_side<T, L::PLANE>(qc, a, 0), load_side<T, L::PLANE>(qc, a + 1, 0)));
+                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 0), load_side<T, L::PLANE_PAD>(qc, a + 1, 0)));
                 } else if (f < L::NFX + L::NFY) {
                     int const g = f - L::NFX;
                     int const fj = g / TX;
                     int const fi = g % TX;
                     int const a = fj * L::HX + fi + 1;
                     store_flux(fy, L::NFY, g, 1,
-                               hllc_flux(load_side<T, L::PLANE>(qc, a, 1), load_side<T, L::PLANE>(qc, a + L::HX, 1)));
+                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 1),
+                                         load_side<T, L::PLANE_PAD>(qc, a + L::HX, 1)));
                 } else {
                     int const g = f - L::NFX - L::NFY;
                     int const fj = g / TX;
                     int const fi = g % TX;
                     int const a = (fj + 1) * L::HX + fi + 1;
                     store_flux(fz, L::NFZ, g, 2,
-                               hllc_flux(load_side<T, L::PLANE>(qc, a, 2), load_side<T, L::PLANE>(qn, a, 2)));
+                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 2), load_side<T, L::PLANE_PAD>(qn, a, 2)));
                 }
             }
-            __syncthreads();
+            if (__syncthreads_or(timed_out)) {
+                break;
+            }
+            if (TMA) {
+                // plane k is no longer read: refill its slot with plane k+3
+                if (k + 3 <= ke) {
+                    if (tid == 0) {
+                        issue_plane<T, TX, TY, NSLOT>(smem, bars, cur, maps, i0, j0, k + 3);
+                    }
+                    inflight |= 1u << cur;
+                }
+            }
 
             // ---- cell phase
             T fza[5];
-            fza[0] = fz[0 * L::NFZ + tid];
-            fza[1] = fz[1 * L::NFZ + tid];
-            fza[2] = fz[2 * L::NFZ + tid];
-            fza[3] = fz[3 * L::NFZ + tid];
-            fza[4] = fz[4 * L::NFZ + tid];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                fza[f] = fz[f * L::NFZ + tid];
+            }
             if (own) {
                 int const xl = tj * (TX + 1) + ti;
                 int const yb = tj * TX + ti;
@@ -235,32 +395,33 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
                     T const ax = fx[f * L::NFX + xl + 1] - fx[f * L::NFX + xl];
                     T const ay = fy[f * L::NFY + yb + TX] - fy[f * L::NFY + yb];
                     T const az = fza[f] - zlo[f];
-                    T acc = ds0 * ax;
-                    acc = acc + ds1 * ay;
-                    acc = acc + ds2 * az;
-                    u[f] = u[f] - dtodv * acc;
+                    u[f] = u[f] - k0 * ax - k1 * ay - k2 * az;
                 }
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
                     p.cons_out.f[f][o] = u[f];
                 }
                 if (MODE == kModeStep) {
-                    T const r = T(1) / u[0];
+                    // cons_to_prim of the new state (cons_to_prim.hpp:26-31)
+                    T const r = rcp_rn(u[0]);
                     T const v0 = u[2] * r;
                     T const v1 = u[3] * r;
                     T const v2 = u[4] * r;
-                    T const ke_ = T(0.5) * r * (u[2] * u[2] + u[3] * u[3] + u[4] * u[4]);
-                    T const pr = p.gm1 * (u[1] - ke_);
-                    T const cs = sqrt(p.gamma * pr * r);
+                    T const mm = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
+                    T const pr = p.gm1 * u[1] - (p.half_gm1 * r) * mm; // (gamma-1)(e - |m|^2/(2 rho))
+                    T const cs = fast_sound_speed((p.gamma * r) * pr);
                     p.prim_out.f[0][o] = u[0];
                     p.prim_out.f[1][o] = pr;
                     p.prim_out.f[2][o] = v0;
                     p.prim_out.f[3][o] = v1;
                     p.prim_out.f[4][o] = v2;
                     p.cs_out[o] = cs;
-                    T const invdt = (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
-                    wmax = (invdt > wmax) ? invdt : wmax;
-                    bad |= !(u[0] > T(0)) || !(pr > T(0)) || !(invdt <= T(3.0e38));
+                    // next step's CFL wavespeed (time_step.hpp:28-33)
+                    T const invdt =
+                            (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
+                    long long const key = wave_key(invdt);
+                    wkey = key > wkey ? key : wkey;
+                    bad |= !cell_ok(u[0], pr, invdt);
                 }
             }
             // the z face above becomes the next plane's z face below
@@ -268,31 +429,53 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(FluxParams<T> p)
             for (int f = 0; f < 5; ++f) {
                 zlo[f] = fza[f];
             }
+            __syncthreads(); // fluxes are rewritten by the next face phase
+        }
+        if (__syncthreads_or(timed_out)) {
+            break;
         }
     }
 
+    if (TMA && __syncthreads_or(timed_out)) {
+        // a staged plane never arrived: report, wait (bounded) for the copies
+        // still in flight so none lands after the CTA is gone, and stop
+        if (tid == 0) {
+            atomicOr(p.status, 2);
+        }
+        for (int s = 0; s < NSLOT; ++s) {
+            if (inflight & (1u << s)) {
+                wait_slot(s);
+            }
+        }
+        return;
+    }
+
     if (MODE == kModeStep) {
-        __shared__ T warp_best[TX * TY / 32];
+        __shared__ long long warp_best[TX * TY / 32];
         __shared__ int any_bad;
         if (tid == 0) {
             any_bad = 0;
         }
-        wmax = warp_max(wmax);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            long long const v = __shfl_xor_sync(0xffffffffu, wkey, o);
+            wkey = v > wkey ? v : wkey;
+        }
         __syncthreads();
         if ((tid & 31) == 0) {
-            warp_best[tid >> 5] = wmax;
+            warp_best[tid >> 5] = wkey;
         }
         if (bad) {
             any_bad = 1;
         }
         __syncthreads();
         if (tid == 0) {
-            T b = warp_best[0];
+            long long b = warp_best[0];
 #pragma unroll
             for (int wv = 1; wv < TX * TY / 32; ++wv) {
-                b = (warp_best[wv] > b) ? warp_best[wv] : b;
+                b = warp_best[wv] > b ? warp_best[wv] : b;
             }
-            atomicMax(p.wmax, order_bits(b));
+            atomicMax(p.wmax, static_cast<unsigned long long>(b));
             if (any_bad) {
                 atomicOr(p.status, 1);
             }
@@ -391,20 +574,56 @@ __global__ void finalize_dt_kernel(SimScalars* s, T cfl, int add_time)
     }
 }
 
+constexpr int kTX = 32;
+constexpr int kTY = 8;
+
+// Chunk length (planes per work item) that balances the persistent grid:
+// the step lasts as long as its busiest CTA, while each extra chunk costs
+// one more z face row and two more staged planes (about 1/(3 kchunk) of a
+// chunk's work).  Scores every length from 8 to 64 by
+//   (planes / (resident CTAs x planes of the busiest CTA)) x (1 - 1/(3 kchunk))
+// and keeps the best.
+int choose_kchunk(int columns, int iz, long long slots)
+{
+    int best = 64;
+    double best_score = -1.0;
+    for (int kc = 8; kc <= 64; ++kc) {
+        long long const chunks = (iz + kc - 1) / kc;
+        long long const items = chunks * columns;
+        long long const rounds = (items + slots - 1) / slots; // items of the busiest CTA
+        double const busiest = static_cast<double>(rounds) * kc;
+        double const score = (static_cast<double>(iz) * columns / (static_cast<double>(slots) * busiest)) *
+                             (1.0 - 1.0 / (3.0 * kc));
+        if (score > best_score + 1e-9) {
+            best_score = score;
+            best = kc;
+        }
+    }
+    return best;
+}
+
+template <class T, int MODE, bool TMA>
+struct FluxKernel {
+    static constexpr int NSLOT = TMA ? 3 : 2;
+    using L = TileLayout<T, kTX, kTY, NSLOT>;
+    static auto fn() { return flux_tile_kernel<T, kTX, kTY, NSLOT, MODE, TMA>; }
+};
+
 // Opts the kernel into its dynamic shared memory size and returns its
 // resident CTAs per SM.  Called outside any stream capture (by the entry
 // points before they enqueue work), and cheap to repeat.
-template <class T, int TX, int TY, int NSLOT, int MODE>
+template <class T, int MODE, bool TMA>
 cudaError_t configure_flux_impl(int* per_sm)
 {
-    using L = TileLayout<T, TX, TY, NSLOT>;
-    auto kern = flux_tile_kernel<T, TX, TY, NSLOT, MODE>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(L::BYTES));
+    using K = FluxKernel<T, MODE, TMA>;
+    auto kern = K::fn();
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(K::L::BYTES));
     if (e != cudaSuccess) {
         return e;
     }
     int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, L::NT, L::BYTES);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, K::L::NT, K::L::BYTES);
     if (e != cudaSuccess) {
         return e;
     }
@@ -412,11 +631,10 @@ cudaError_t configure_flux_impl(int* per_sm)
     return cudaSuccess;
 }
 
-template <class T, int TX, int TY, int NSLOT, int MODE>
-cudaError_t launch_flux_impl(FluxParams<T> p, int sms, cudaStream_t s)
+template <class T, int MODE, bool TMA>
+cudaError_t launch_flux_impl(FluxParams<T> p, TmaMaps const& maps, int sms, cudaStream_t s)
 {
-    using L = TileLayout<T, TX, TY, NSLOT>;
-    auto kern = flux_tile_kernel<T, TX, TY, NSLOT, MODE>;
+    using K = FluxKernel<T, MODE, TMA>;
     int const per_sm = p.per_sm > 0 ? p.per_sm : 1;
     int const ix = p.g.n0 - 2;
     int const iy = p.g.n1 - 2;
@@ -424,40 +642,44 @@ cudaError_t launch_flux_impl(FluxParams<T> p, int sms, cudaStream_t s)
     if (ix <= 0 || iy <= 0 || iz <= 0) {
         return cudaSuccess; // no interior cell
     }
-    p.tiles_x = (ix + TX - 1) / TX;
-    p.tiles_y = (iy + TY - 1) / TY;
+    p.tiles_x = (ix + kTX - 1) / kTX;
+    p.tiles_y = (iy + kTY - 1) / kTY;
+    long long const slots = static_cast<long long>(sms) * per_sm;
     if (p.kchunk <= 0) {
-        p.kchunk = 32;
+        p.kchunk = choose_kchunk(p.tiles_x * p.tiles_y, iz, slots);
     }
     int const kchunks = (iz + p.kchunk - 1) / p.kchunk;
     long long const nwork = static_cast<long long>(p.tiles_x) * p.tiles_y * kchunks;
     p.nwork = static_cast<int>(nwork);
-    long long grid = static_cast<long long>(sms) * per_sm;
+    long long grid = slots;
     if (grid > nwork) {
         grid = nwork;
     }
-    kern<<<static_cast<int>(grid), L::NT, L::BYTES, s>>>(p);
+    K::fn()<<<static_cast<int>(grid), K::L::NT, K::L::BYTES, s>>>(p, maps);
     return cudaGetLastError();
 }
 
 } // namespace
 
 template <class T>
-cudaError_t configure_flux(int mode, int* per_sm)
+cudaError_t configure_flux(int mode, bool tma, int* per_sm)
 {
     if (mode == kModeStep) {
-        return configure_flux_impl<T, 32, 8, 2, kModeStep>(per_sm);
+        return tma ? configure_flux_impl<T, kModeStep, true>(per_sm) : configure_flux_impl<T, kModeStep, false>(per_sm);
     }
-    return configure_flux_impl<T, 32, 8, 2, kModeGodunov>(per_sm);
+    return configure_flux_impl<T, kModeGodunov, false>(per_sm);
 }
 
 template <class T>
-cudaError_t launch_flux(FluxParams<T> p, int mode, int sms, cudaStream_t s)
+cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int sms, cudaStream_t s)
 {
     if (mode == kModeStep) {
-        return launch_flux_impl<T, 32, 8, 2, kModeStep>(p, sms, s);
+        if (maps != nullptr) {
+            return launch_flux_impl<T, kModeStep, true>(p, *maps, sms, s);
+        }
+        return launch_flux_impl<T, kModeStep, false>(p, TmaMaps{}, sms, s);
     }
-    return launch_flux_impl<T, 32, 8, 2, kModeGodunov>(p, sms, s);
+    return launch_flux_impl<T, kModeGodunov, false>(p, TmaMaps{}, sms, s);
 }
 
 template <class T>
@@ -489,10 +711,13 @@ cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t
     return cudaGetLastError();
 }
 
-template cudaError_t configure_flux<double>(int, int*);
-template cudaError_t configure_flux<float>(int, int*);
-template cudaError_t launch_flux<double>(FluxParams<double>, int, int, cudaStream_t);
-template cudaError_t launch_flux<float>(FluxParams<float>, int, int, cudaStream_t);
+int flux_tile_x() { return kTX; }
+int flux_tile_y() { return kTY; }
+
+template cudaError_t configure_flux<double>(int, bool, int*);
+template cudaError_t configure_flux<float>(int, bool, int*);
+template cudaError_t launch_flux<double>(FluxParams<double>, TmaMaps const*, int, int, cudaStream_t);
+template cudaError_t launch_flux<float>(FluxParams<float>, TmaMaps const*, int, int, cudaStream_t);
 template cudaError_t launch_ghost_shell<double>(GhostParams<double>, int, cudaStream_t);
 template cudaError_t launch_ghost_shell<float>(GhostParams<float>, int, cudaStream_t);
 template cudaError_t launch_finalize_dt<double>(SimScalars*, double, int, cudaStream_t);

@@ -1,6 +1,7 @@
 // Host-side launch interface of the Euler kernels (internal to the library).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "euler_device.cuh"
@@ -20,6 +21,12 @@ struct SimScalars {
     int pad;
 };
 
+// TMA descriptors of the seven staged fields (d, p, u0, u1, u2, c, e) of the
+// step's input copy: 3D tensors (n0, n1, n2), boxes of (TX+2) x (TY+2) x 1.
+struct TmaMaps {
+    CUtensorMap m[7];
+};
+
 template <class T>
 struct FluxParams {
     Geom g;
@@ -29,7 +36,7 @@ struct FluxParams {
     Bundle<T> cons_out;  // written (interior); may equal cons_in in godunov mode
     Bundle<T> prim_out;  // step mode: cons_to_prim of the new state (interior)
     T* cs_out;           // step mode: sound speed of the new state (interior)
-    T gamma, gm1, inv_gm1;
+    T gamma, gm1, inv_gm1, half_gm1;
     T ds0, ds1, ds2;     // face areas dx1*dx2, dx2*dx0, dx0*dx1
     T dv;                // cell volume
     T dtodv;             // dt/dv when dt_dev is null
@@ -70,9 +77,12 @@ template <class T>
 cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s);
 
 template <class T>
-cudaError_t configure_flux(int mode, int* per_sm);
+cudaError_t configure_flux(int mode, bool tma, int* per_sm);
+// maps != nullptr selects TMA staging (step mode only)
 template <class T>
-cudaError_t launch_flux(FluxParams<T> p, int mode, int sms, cudaStream_t s);
+cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int sms, cudaStream_t s);
+int flux_tile_x();
+int flux_tile_y();
 template <class T>
 cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s);
 template <class T>

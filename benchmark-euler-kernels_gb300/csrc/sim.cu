@@ -15,7 +15,10 @@
 #include "euler_gb300.h"
 #include "kernels.h"
 
+#include <cudaTypedefs.h>
+
 #include <cmath>
+#include <mutex>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -77,6 +80,8 @@ struct eulr_sim {
     double* totals = nullptr;
     int cur = 0;
     int per_sm = 1; // resident CTAs per SM of the step kernel
+    bool tma = false; // stage planes by TMA (row pitch a multiple of 16 bytes)
+    TmaMaps maps[2] = {}; // descriptors of copy 0 and copy 1 as step input
     bool loaded = false;
     cudaGraphExec_t graph = nullptr;
 };
@@ -97,6 +102,65 @@ int check_sim(eulr_sim* s)
 }
 
 long long ncell(eulr_sim const* s) { return s->g.ncell(); }
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link-time dependency on libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                    cudaSuccess &&
+            q == cudaDriverEntryPointSuccess) {
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        }
+    });
+    return fn;
+}
+
+// 3D tensor (n0, n1, n2) of doubles, layout_left, box (TX+2, TY+2, 1).
+// Requires the row pitch n0*8 to be a multiple of 16 bytes and a 16-byte
+// aligned base (fields are 256-byte aligned in the simulation's allocation).
+bool encode_field_map(CUtensorMap* m, double* base, Geom const& g)
+{
+    auto enc = tensor_map_encoder();
+    if (enc == nullptr) {
+        return false;
+    }
+    cuuint64_t dims[3] = {static_cast<cuuint64_t>(g.n0), static_cast<cuuint64_t>(g.n1),
+                          static_cast<cuuint64_t>(g.n2)};
+    cuuint64_t strides[2] = {static_cast<cuuint64_t>(g.s1) * sizeof(double),
+                             static_cast<cuuint64_t>(g.s2) * sizeof(double)};
+    cuuint32_t box[3] = {static_cast<cuuint32_t>(flux_tile_x() + 2), static_cast<cuuint32_t>(flux_tile_y() + 2), 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult const r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+// TMA staging needs 16-byte row and plane pitches; the descriptors of both
+// copies are built once.  On any failure the plain-load staging is used.
+void setup_tma(eulr_sim* s)
+{
+    s->tma = false;
+    if ((static_cast<size_t>(s->g.n0) * sizeof(double)) % 16 != 0) {
+        return;
+    }
+    for (int c = 0; c < 2; ++c) {
+        double* f[7] = {s->prim[c][0], s->prim[c][1], s->prim[c][2], s->prim[c][3], s->prim[c][4], s->cs[c],
+                        s->cons[c][1]};
+        for (int i = 0; i < 7; ++i) {
+            if (!encode_field_map(&s->maps[c].m[i], f[i], s->g)) {
+                return;
+            }
+        }
+    }
+    s->tma = true;
+}
 
 // One fused step from copy `in` to copy `1-in`; with `ev` (4 events) the
 // launches are bracketed for per-kernel timing.
@@ -133,6 +197,7 @@ int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
     p.gamma = s->gamma;
     p.gm1 = s->gamma - 1.0;
     p.inv_gm1 = 1.0 / (s->gamma - 1.0);
+    p.half_gm1 = 0.5 * (s->gamma - 1.0);
     p.ds0 = s->dx[1] * s->dx[2];
     p.ds1 = s->dx[2] * s->dx[0];
     p.ds2 = s->dx[0] * s->dx[1];
@@ -148,7 +213,7 @@ int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[1], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_flux<double>(p, kModeStep, s->sms, s->stream), "step launch");
+    SIM_CUDA(launch_flux<double>(p, s->tma ? &s->maps[in] : nullptr, kModeStep, s->sms, s->stream), "step launch");
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[2], s->stream), "cudaEventRecord");
     }
@@ -243,10 +308,6 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
     if (e != cudaSuccess) {
         return bail(cfail(e, "cudaDeviceGetAttribute"));
     }
-    e = configure_flux<double>(kModeStep, &s->per_sm);
-    if (e != cudaSuccess) {
-        return bail(cfail(e, "step kernel configure"));
-    }
     if (stream != nullptr) {
         s->stream = stream;
     } else {
@@ -280,6 +341,11 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
     s->sc = reinterpret_cast<SimScalars*>(b);
     b += scal;
     s->totals = reinterpret_cast<double*>(b);
+    setup_tma(s);
+    e = configure_flux<double>(kModeStep, s->tma, &s->per_sm);
+    if (e != cudaSuccess) {
+        return bail(cfail(e, "step kernel configure"));
+    }
     e = cudaMemsetAsync(s->sc, 0, sizeof(SimScalars), s->stream);
     if (e != cudaSuccess) {
         return bail(cfail(e, "cudaMemsetAsync"));
