@@ -65,6 +65,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ops", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-fp32c", action="store_true")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="implosion, FP32 states vs the plain FP64 run (L1/Linf of rho, p, |u|); prints its own JSON")
+    ap.add_argument("--study-n", type=int, nargs="+", default=[512, 768])
+    ap.add_argument("--study-steps", type=int, default=1000)
     return ap.parse_args()
 
 
@@ -205,6 +210,114 @@ def random_prim_device(torch, n0, n1, n2, seed=0):
     return prim
 
 
+def rel_errors(torch, a, b):
+    """Relative L1 (sum|a-b|/sum|b|) and Linf (max|a-b|/max|b|) over interior cells."""
+    a = a[1:-1, 1:-1, 1:-1]
+    b = b[1:-1, 1:-1, 1:-1]
+    d = (a - b).abs()
+    return (d.sum() / b.abs().sum()).item(), (d.max() / b.abs().max()).item()
+
+
+def state_errors(torch, prim, prim_ref):
+    """L1/Linf of rho, p and |u| of prim against prim_ref (device tensors)."""
+    out = {}
+    for name, f in (("rho", 0), ("p", 1)):
+        l1, li = rel_errors(torch, prim[f], prim_ref[f])
+        out[name] = {"l1": l1, "linf": li}
+    speed = prim[2:5].square().sum(0).sqrt()
+    speed_ref = prim_ref[2:5].square().sum(0).sqrt()
+    l1, li = rel_errors(torch, speed, speed_ref)
+    out["|u|"] = {"l1": l1, "linf": li}
+    return out
+
+
+def run_fp32c_leg(torch, E, args, stream, n0, dx, interior, steps_total, prim_ref, hbm_peak):
+    """The FP32-compensated state on the same workload: throughput, HBM
+    roofline and the error against the FP64 state after the same steps."""
+    prim = random_prim_device(torch, n0, n0, n0, seed=0)
+    out = {}
+    with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, precision="f32c", stream=stream) as sim:
+        sim.set_prim(prim)
+        del prim
+        for _ in range(args.warmup):
+            sim.advance(1)
+        prof = [sim.profile_step() for _ in range(3)]
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        sim.advance(args.steps)
+        e.record(stream)
+        e.synchronize()
+        ms = s.elapsed_time(e)
+        assert args.warmup + 3 + args.steps == steps_total
+        got = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
+        sim.get_state(prim=got)
+        status = sim.status()
+        bytes_step = sim.state_bytes()
+    flux_ms = min(p[1] for p in prof)
+    err = state_errors(torch, got, prim_ref)
+    del got
+    torch.cuda.empty_cache()
+    out = {"value": interior * args.steps / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms / args.steps,
+           "precision": "f32c: FP32 state, FP32 HLLC, compensated update (error-free sum of cell + six face "
+                        "terms, one rounding), FP64 internal energy for low-pressure cells",
+           "errors_vs_f64": err, "errors_after_steps": steps_total, "status": status,
+           "roofline": {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes_per_cell": bytes_step / interior,
+                        "achieved": bytes_step / (flux_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                        "peak_source": "MEASURED_PEAKS.json (measured)" if hbm_peak else None,
+                        "kernel_ms": flux_ms}}
+    if hbm_peak:
+        out["roofline"]["frac"] = out["roofline"]["achieved"] / hbm_peak
+    return out
+
+
+def run_precision_study(args):
+    """Implosion (init_implode) at each N for study-steps steps: FP32 states
+    against the plain FP64 run, L1/Linf of rho, p, |u|."""
+    import torch
+
+    import euler_gb300 as E
+
+    E.build()
+    E.load()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    results = []
+    for n in args.study_n:
+        n0 = n + 2
+        dx = (1.0 / n,) * 3
+        rec = {"n": n, "steps": args.study_steps}
+        with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, precision="f64", stream=stream) as sim:
+            sim.init_implode()
+            t0 = time.perf_counter()
+            sim.advance(args.study_steps)
+            torch.cuda.synchronize()
+            rec["f64_seconds"] = time.perf_counter() - t0
+            ref = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
+            sim.get_state(prim=ref)
+            rec["t_final"] = sim.time()[0]
+            rec["f64_totals"] = sim.totals()
+        torch.cuda.empty_cache()
+        for precision in ("f32c", "f32c_hilo", "f32"):
+            with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, precision=precision, stream=stream) as sim:
+                sim.init_implode()
+                t0 = time.perf_counter()
+                sim.advance(args.study_steps)
+                torch.cuda.synchronize()
+                el = time.perf_counter() - t0
+                got = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
+                sim.get_state(prim=got)
+                rec[precision] = {"seconds": el, "t_final": sim.time()[0], "status": sim.status(),
+                                  "totals": sim.totals(), "errors": state_errors(torch, got, ref)}
+                del got
+            torch.cuda.empty_cache()
+        del ref
+        torch.cuda.empty_cache()
+        results.append(rec)
+        print(json.dumps({"precision_study": rec}), flush=True)
+    return 0
+
+
 def time_ops(torch, E, prim, n_int):
     """Each reference operator alone, one call after warm-up (CUDA events)."""
     n0 = n_int + 2
@@ -339,6 +452,15 @@ def run_ours(args):
         hbm["frac"] = hbm["achieved_gbs"] / hbm_peak
     roof["hbm"] = hbm
 
+    fp32c = None
+    if not args.no_fp32c:
+        ref = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
+        sim.get_state(prim=ref)
+        fp32c = run_fp32c_leg(torch, E, args, stream, n0, dx, interior, args.warmup + 3 + args.steps, ref, hbm_peak)
+        fp32c["speedup_vs_f64"] = fp32c["value"] / value
+        del ref
+        torch.cuda.empty_cache()
+
     ops = None
     if not args.no_ops and rank == 0:
         prim = random_prim_device(torch, n0, n0, n0, seed=1)
@@ -395,6 +517,7 @@ def run_ours(args):
             "clocks": clk,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "fp32c": fp32c,
             "operators": ops,
             "status": status,
             "sim": {"t": t_sim, "steps_taken": nsteps},
@@ -410,6 +533,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.precision_study:
+        return run_precision_study(args)
     return run_ours(args)
 
 

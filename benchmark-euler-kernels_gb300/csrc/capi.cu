@@ -311,12 +311,16 @@ int godunov_impl(PB prim, CB cons, int n0, int n1, int n2, T gamma, T dx0, T dx1
     p.ds0 = dx1 * dx2; // uniform_mesh.hpp:62-75
     p.ds1 = dx2 * dx0;
     p.ds2 = dx0 * dx1;
-    p.dv = dx0 * dx1 * dx2;
-    p.dtodv = dt / p.dv;
-    p.dt_dev = dt_dev;
-    p.cfl = cfl;
-    EULR_CUDA_TRY(configure_flux<T>(kModeGodunov, false, &p.per_sm), "godunov configure");
-    EULR_CUDA_TRY(launch_flux<T>(p, nullptr, kModeGodunov, sms, s), "godunov launch");
+    p.dv = static_cast<double>(dx0 * dx1 * dx2);
+    p.dtodv = dt / (dx0 * dx1 * dx2);
+    if constexpr (sizeof(T) == sizeof(double)) {
+        p.dt_dev = dt_dev; // the device-dt variant exists for FP64 only
+    } else {
+        p.dt_dev = nullptr;
+    }
+    p.cfl = static_cast<double>(cfl);
+    EULR_CUDA_TRY(configure_flux<T>(kModeGodunov, false, kCompNone, &p.per_sm), "godunov configure");
+    EULR_CUDA_TRY(launch_flux<T>(p, nullptr, kModeGodunov, kCompNone, sms, s), "godunov launch");
     return EULR_SUCCESS;
 }
 

@@ -130,6 +130,32 @@ __device__ __forceinline__ T cell_invdt_exact(T d, T p, T u0, T u1, T u2, T gamm
     return add_rn(add_rn(mul_rn(c0, ix0), mul_rn(c1, ix1)), mul_rn(c2, ix2));
 }
 
+// ------------------------------------------- FP32 cons_to_prim with FP64 rescue
+// Below this fraction of e the FP32 internal-energy subtraction
+// e - |m|^2/(2 rho) has lost more than 8 of its 24 bits.
+constexpr float kLowPressure = 1.0f / 256.0f;
+
+// Pressure of an FP32 conservative state: the subtraction runs in FP32
+// unless the cell's internal energy is below kLowPressure of its total
+// energy, where it is redone in FP64 from the FP32 words (hi, plus the low
+// words when the state stores them).
+__device__ __forceinline__ float pressure_f32c(float d, float e, float m0, float m1, float m2, float r, float gm1,
+                                               const float* lo)
+{
+    float const mm = m0 * m0 + m1 * m1 + m2 * m2;
+    float const eint = e - (0.5f * r) * mm;
+    if (eint > kLowPressure * e) {
+        return gm1 * eint;
+    }
+    double const dd = static_cast<double>(d) + (lo ? static_cast<double>(lo[0]) : 0.0);
+    double const ed = static_cast<double>(e) + (lo ? static_cast<double>(lo[1]) : 0.0);
+    double const a0 = static_cast<double>(m0) + (lo ? static_cast<double>(lo[2]) : 0.0);
+    double const a1 = static_cast<double>(m1) + (lo ? static_cast<double>(lo[3]) : 0.0);
+    double const a2 = static_cast<double>(m2) + (lo ? static_cast<double>(lo[4]) : 0.0);
+    double const ke = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2) / dd;
+    return static_cast<float>(static_cast<double>(gm1) * (ed - ke));
+}
+
 // ------------------------------------------------------------------ HLLC
 // One side of a face in the face's frame: normal velocity un, tangential
 // velocities ut1/ut2 (in the cyclic order of the axes after the normal), sound

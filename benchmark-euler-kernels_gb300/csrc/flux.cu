@@ -117,6 +117,28 @@ __device__ __forceinline__ T* slot_field(T* smem, int slot, int field)
     return smem + (slot * kFields + field) * L::PLANE_PAD;
 }
 
+// Pressure of an FP32 conservative state: compensated states rescue the
+// low-pressure cells in FP64 (pressure_f32c), plain FP32 does not.
+template <int COMP>
+__device__ __forceinline__ float cons_pressure(float d, float e, float m0, float m1, float m2, float r, float gm1,
+                                               const float* lo)
+{
+    if (COMP != kCompNone) {
+        return pressure_f32c(d, e, m0, m1, m2, r, gm1, lo);
+    }
+    return gm1 * (e - (0.5f * r) * (m0 * m0 + m1 * m1 + m2 * m2));
+}
+template <int COMP>
+__device__ __forceinline__ double cons_pressure(double, double, double, double, double, double, double, const double*)
+{
+    return 0.0;
+}
+
+// Sound speed sqrt(gamma p / rho) = x * rsqrt(x): rsqrt costs fewer FP64
+// instructions than a correctly rounded sqrt; the result is within ~2 ulps.
+__device__ __forceinline__ double fast_sound_speed(double c2) { return c2 * rsqrt(c2); }
+__device__ __forceinline__ float fast_sound_speed(float c2) { return c2 * rsqrtf(c2); }
+
 // Issue the TMA loads of plane k (x origin i0-1, y origin j0-1) into `slot`.
 template <class T, int TX, int TY, int NSLOT>
 __device__ __forceinline__ void issue_plane(T* smem, unsigned long long* bars, int slot, TmaMaps const& maps, int i0,
@@ -135,7 +157,7 @@ __device__ __forceinline__ void issue_plane(T* smem, unsigned long long* bars, i
 // step mode reads the stored sound speed and the conservative energy.  Cells
 // outside the array get a benign uniform state; no face touching them is
 // ever used.
-template <class T, int TX, int TY, int NSLOT, int MODE>
+template <class T, int TX, int TY, int NSLOT, int MODE, int COMP>
 __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> const& p, int i0, int j0, int k)
 {
     using L = TileLayout<T, TX, TY, NSLOT>;
@@ -148,14 +170,29 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
         T d = T(1), pr = T(1), u0 = T(0), u1 = T(0), u2 = T(0), cs = T(1), e = T(2.5);
         if (i < p.g.n0 && j < p.g.n1) {
             long long const o = p.g.at(i, j, k);
-            d = __ldg(p.prim.f[0] + o);
-            pr = __ldg(p.prim.f[1] + o);
-            u0 = __ldg(p.prim.f[2] + o);
-            u1 = __ldg(p.prim.f[3] + o);
-            u2 = __ldg(p.prim.f[4] + o);
+            if (MODE != kModeStepCons) {
+                d = __ldg(p.prim.f[0] + o);
+                pr = __ldg(p.prim.f[1] + o);
+                u0 = __ldg(p.prim.f[2] + o);
+                u1 = __ldg(p.prim.f[3] + o);
+                u2 = __ldg(p.prim.f[4] + o);
+            }
             if (MODE == kModeStep) {
                 cs = __ldg(p.cs + o);
                 e = __ldg(p.cons_in.f[1] + o);
+            } else if (MODE == kModeStepCons) {
+                // cons-only FP32 state: cons_to_prim on chip
+                T const m0 = __ldg(p.cons_in.f[2] + o);
+                T const m1 = __ldg(p.cons_in.f[3] + o);
+                T const m2 = __ldg(p.cons_in.f[4] + o);
+                d = __ldg(p.cons_in.f[0] + o);
+                e = __ldg(p.cons_in.f[1] + o);
+                T const r = T(1) / d;
+                u0 = m0 * r;
+                u1 = m1 * r;
+                u2 = m2 * r;
+                pr = cons_pressure<COMP>(d, e, m0, m1, m2, r, p.gm1, nullptr);
+                cs = fast_sound_speed(p.gamma * pr * r);
             } else {
                 T const r = T(1) / d;
                 cs = sqrt(p.gamma * pr * r);
@@ -196,11 +233,6 @@ __device__ __forceinline__ void store_flux(T* out, int stride, int idx, int dir,
     out[(2 + (dir + 2) % 3) * stride + idx] = f.t2;
 }
 
-// Sound speed sqrt(gamma p / rho) = x * rsqrt(x): rsqrt costs fewer FP64
-// instructions than a correctly rounded sqrt; the result is within ~2 ulps.
-__device__ __forceinline__ double fast_sound_speed(double c2) { return c2 * rsqrt(c2); }
-__device__ __forceinline__ float fast_sound_speed(float c2) { return c2 * rsqrtf(c2); }
-
 __device__ __forceinline__ long long wave_key(double v)
 {
     long long const b = dbits(v);
@@ -217,10 +249,25 @@ __device__ __forceinline__ bool cell_ok(float d, float pr, float invdt)
     return d > 0.0f && pr > 0.0f && invdt <= 3.0e38f;
 }
 
-template <class T, int TX, int TY, int NSLOT, int MODE, bool TMA>
+// sum + err += k*f without rounding error in the product (TwoProduct via
+// FMA) or in the running sum (Knuth's TwoSum); the errors collect in err.
+__device__ __forceinline__ void compensated_add(float& sum, float& err, float k, float f)
+{
+    float const prod = k * f;
+    float const prod_err = fmaf(k, f, -prod);
+    float const s = sum + prod;
+    float const bb = s - sum;
+    float const sum_err = (sum - (s - bb)) + (prod - bb);
+    sum = s;
+    err += sum_err + prod_err;
+}
+__device__ __forceinline__ void compensated_add(double&, double&, double, double) {}
+
+template <class T, int TX, int TY, int NSLOT, int MODE, bool TMA, int COMP>
 __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant__ FluxParams<T> p,
                                                            const __grid_constant__ TmaMaps maps)
 {
+    static_assert(COMP == kCompNone || (sizeof(T) == 4 && MODE == kModeStepCons), "compensation is for the FP32 step");
     using L = TileLayout<T, TX, TY, NSLOT>;
     static_assert(!TMA || NSLOT == 3, "the TMA ring has three slots");
     extern __shared__ __align__(128) unsigned char smem_dyn[];
@@ -234,8 +281,8 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant
 
     T dtodv = p.dtodv;
     if (p.dt_dev != nullptr) {
-        T const dtc = p.cfl * *p.dt_dev; // cfl * dt, euler_simulation.cpp:65
-        dtodv = dtc / p.dv;              // godunov.hpp:37
+        double const dtc = p.cfl * *p.dt_dev;    // cfl * dt, euler_simulation.cpp:65
+        dtodv = static_cast<T>(dtc / p.dv);      // godunov.hpp:37
     }
     // cons -= dt/dv * sum_d ds_d (F_R - F_L), coefficients folded
     T const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2;
@@ -293,8 +340,8 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant
             timed_out |= !wait_slot(0);
             timed_out |= !wait_slot(1);
         } else {
-            load_plane<T, TX, TY, NSLOT, MODE>(smem, 0, p, i0, j0, kb - 1);
-            load_plane<T, TX, TY, NSLOT, MODE>(smem, 1, p, i0, j0, kb);
+            load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, 0, p, i0, j0, kb - 1);
+            load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, 1, p, i0, j0, kb);
             __syncthreads();
         }
         // z face below the chunk's first plane, kept in registers in global
@@ -327,17 +374,21 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant
             int const nxt = (k - kb + 2) % NSLOT;
             // this cell's conservative state, fetched while the faces are solved
             T u[5];
+            T ulo[5] = {T(0), T(0), T(0), T(0), T(0)};
             long long const o = p.g.at(i, j, k);
             if (own) {
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
                     u[f] = p.cons_in.f[f][o];
+                    if (COMP == kCompHiLo) {
+                        ulo[f] = p.lo_in.f[f][o];
+                    }
                 }
             }
             if (TMA) {
                 timed_out |= !wait_slot(nxt);
             } else {
-                load_plane<T, TX, TY, NSLOT, MODE>(smem, nxt, p, i0, j0, k + 1);
+                load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, nxt, p, i0, j0, k + 1);
                 __syncthreads();
             }
 
@@ -392,30 +443,57 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant
                 int const yb = tj * TX + ti;
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    T const ax = fx[f * L::NFX + xl + 1] - fx[f * L::NFX + xl];
-                    T const ay = fy[f * L::NFY + yb + TX] - fy[f * L::NFY + yb];
-                    T const az = fza[f] - zlo[f];
-                    u[f] = u[f] - k0 * ax - k1 * ay - k2 * az;
+                    if (COMP == kCompNone) {
+                        T const ax = fx[f * L::NFX + xl + 1] - fx[f * L::NFX + xl];
+                        T const ay = fy[f * L::NFY + yb + TX] - fy[f * L::NFY + yb];
+                        T const az = fza[f] - zlo[f];
+                        u[f] = u[f] - k0 * ax - k1 * ay - k2 * az;
+                    } else {
+                        // cons + six signed face terms, summed without
+                        // intermediate rounding error (TwoProduct +
+                        // TwoSum), then rounded once
+                        T sum = u[f];
+                        T err = ulo[f];
+                        compensated_add(sum, err, -k0, fx[f * L::NFX + xl + 1]);
+                        compensated_add(sum, err, k0, fx[f * L::NFX + xl]);
+                        compensated_add(sum, err, -k1, fy[f * L::NFY + yb + TX]);
+                        compensated_add(sum, err, k1, fy[f * L::NFY + yb]);
+                        compensated_add(sum, err, -k2, fza[f]);
+                        compensated_add(sum, err, k2, zlo[f]);
+                        u[f] = sum + err;
+                        ulo[f] = err - (u[f] - sum);
+                    }
                 }
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
                     p.cons_out.f[f][o] = u[f];
+                    if (COMP == kCompHiLo) {
+                        p.lo_out.f[f][o] = ulo[f];
+                    }
                 }
-                if (MODE == kModeStep) {
+                if (MODE == kModeStep || MODE == kModeStepCons) {
                     // cons_to_prim of the new state (cons_to_prim.hpp:26-31)
                     T const r = rcp_rn(u[0]);
                     T const v0 = u[2] * r;
                     T const v1 = u[3] * r;
                     T const v2 = u[4] * r;
-                    T const mm = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
-                    T const pr = p.gm1 * u[1] - (p.half_gm1 * r) * mm; // (gamma-1)(e - |m|^2/(2 rho))
+                    T pr;
+                    if (MODE == kModeStep) {
+                        T const mm = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
+                        pr = p.gm1 * u[1] - (p.half_gm1 * r) * mm; // (gamma-1)(e - |m|^2/(2 rho))
+                    } else {
+                        pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1,
+                                                 COMP == kCompHiLo ? ulo : nullptr);
+                    }
                     T const cs = fast_sound_speed((p.gamma * r) * pr);
-                    p.prim_out.f[0][o] = u[0];
-                    p.prim_out.f[1][o] = pr;
-                    p.prim_out.f[2][o] = v0;
-                    p.prim_out.f[3][o] = v1;
-                    p.prim_out.f[4][o] = v2;
-                    p.cs_out[o] = cs;
+                    if (MODE == kModeStep) {
+                        p.prim_out.f[0][o] = u[0];
+                        p.prim_out.f[1][o] = pr;
+                        p.prim_out.f[2][o] = v0;
+                        p.prim_out.f[3][o] = v1;
+                        p.prim_out.f[4][o] = v2;
+                        p.cs_out[o] = cs;
+                    }
                     // next step's CFL wavespeed (time_step.hpp:28-33)
                     T const invdt =
                             (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
@@ -450,7 +528,7 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant
         return;
     }
 
-    if (MODE == kModeStep) {
+    if (MODE == kModeStep || MODE == kModeStepCons) {
         __shared__ long long warp_best[TX * TY / 32];
         __shared__ int any_bad;
         if (tid == 0) {
@@ -526,18 +604,36 @@ __global__ void __launch_bounds__(256) ghost_shell_kernel(GhostParams<T> p)
         T const m1 = p.cons_in.f[3][o];
         T const m2 = p.cons_in.f[4][o];
         T pr, u0, u1, u2;
-        cons_to_prim_exact(d, e, m0, m1, m2, p.gm1, pr, u0, u1, u2);
+        if (p.prim_out.f[0] == nullptr) {
+            // cons-only FP32 state: only the cons words and the wavespeed
+            T const r = T(1) / d;
+            u0 = m0 * r;
+            u1 = m1 * r;
+            u2 = m2 * r;
+            pr = p.comp != kCompNone ? cons_pressure<kCompSum>(d, e, m0, m1, m2, r, p.gm1, nullptr)
+                                     : cons_pressure<kCompNone>(d, e, m0, m1, m2, r, p.gm1, nullptr);
+        } else {
+            cons_to_prim_exact(d, e, m0, m1, m2, p.gm1, pr, u0, u1, u2);
+        }
         p.cons_out.f[0][o] = d;
         p.cons_out.f[1][o] = e;
         p.cons_out.f[2][o] = m0;
         p.cons_out.f[3][o] = m1;
         p.cons_out.f[4][o] = m2;
-        p.prim_out.f[0][o] = d;
-        p.prim_out.f[1][o] = pr;
-        p.prim_out.f[2][o] = u0;
-        p.prim_out.f[3][o] = u1;
-        p.prim_out.f[4][o] = u2;
-        p.cs_out[o] = sqrt_rn(div_rn(mul_rn(p.gamma, pr), d));
+        if (p.lo_in.f[0] != nullptr) {
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                p.lo_out.f[f][o] = p.lo_in.f[f][o];
+            }
+        }
+        if (p.prim_out.f[0] != nullptr) {
+            p.prim_out.f[0][o] = d;
+            p.prim_out.f[1][o] = pr;
+            p.prim_out.f[2][o] = u0;
+            p.prim_out.f[3][o] = u1;
+            p.prim_out.f[4][o] = u2;
+            p.cs_out[o] = sqrt_rn(div_rn(mul_rn(p.gamma, pr), d));
+        }
         T const v = cell_invdt_exact(d, pr, u0, u1, u2, p.gamma, p.invdx0, p.invdx1, p.invdx2);
         wmax = (v > wmax) ? v : wmax;
     }
@@ -602,20 +698,20 @@ int choose_kchunk(int columns, int iz, long long slots)
     return best;
 }
 
-template <class T, int MODE, bool TMA>
+template <class T, int MODE, bool TMA, int COMP>
 struct FluxKernel {
     static constexpr int NSLOT = TMA ? 3 : 2;
     using L = TileLayout<T, kTX, kTY, NSLOT>;
-    static auto fn() { return flux_tile_kernel<T, kTX, kTY, NSLOT, MODE, TMA>; }
+    static auto fn() { return flux_tile_kernel<T, kTX, kTY, NSLOT, MODE, TMA, COMP>; }
 };
 
 // Opts the kernel into its dynamic shared memory size and returns its
 // resident CTAs per SM.  Called outside any stream capture (by the entry
 // points before they enqueue work), and cheap to repeat.
-template <class T, int MODE, bool TMA>
+template <class T, int MODE, bool TMA, int COMP>
 cudaError_t configure_flux_impl(int* per_sm)
 {
-    using K = FluxKernel<T, MODE, TMA>;
+    using K = FluxKernel<T, MODE, TMA, COMP>;
     auto kern = K::fn();
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(K::L::BYTES));
@@ -631,10 +727,10 @@ cudaError_t configure_flux_impl(int* per_sm)
     return cudaSuccess;
 }
 
-template <class T, int MODE, bool TMA>
+template <class T, int MODE, bool TMA, int COMP>
 cudaError_t launch_flux_impl(FluxParams<T> p, TmaMaps const& maps, int sms, cudaStream_t s)
 {
-    using K = FluxKernel<T, MODE, TMA>;
+    using K = FluxKernel<T, MODE, TMA, COMP>;
     int const per_sm = p.per_sm > 0 ? p.per_sm : 1;
     int const ix = p.g.n0 - 2;
     int const iy = p.g.n1 - 2;
@@ -662,24 +758,68 @@ cudaError_t launch_flux_impl(FluxParams<T> p, TmaMaps const& maps, int sms, cuda
 } // namespace
 
 template <class T>
-cudaError_t configure_flux(int mode, bool tma, int* per_sm)
-{
-    if (mode == kModeStep) {
-        return tma ? configure_flux_impl<T, kModeStep, true>(per_sm) : configure_flux_impl<T, kModeStep, false>(per_sm);
+struct FluxDispatch;
+
+template <>
+struct FluxDispatch<double> {
+    static cudaError_t configure(int mode, bool tma, int /*comp*/, int* per_sm)
+    {
+        if (mode == kModeStep) {
+            return tma ? configure_flux_impl<double, kModeStep, true, kCompNone>(per_sm)
+                       : configure_flux_impl<double, kModeStep, false, kCompNone>(per_sm);
+        }
+        return configure_flux_impl<double, kModeGodunov, false, kCompNone>(per_sm);
     }
-    return configure_flux_impl<T, kModeGodunov, false>(per_sm);
+    static cudaError_t launch(FluxParams<double> const& p, TmaMaps const* maps, int mode, int /*comp*/, int sms,
+                              cudaStream_t s)
+    {
+        if (mode == kModeStep) {
+            if (maps != nullptr) {
+                return launch_flux_impl<double, kModeStep, true, kCompNone>(p, *maps, sms, s);
+            }
+            return launch_flux_impl<double, kModeStep, false, kCompNone>(p, TmaMaps{}, sms, s);
+        }
+        return launch_flux_impl<double, kModeGodunov, false, kCompNone>(p, TmaMaps{}, sms, s);
+    }
+};
+
+template <>
+struct FluxDispatch<float> {
+    static cudaError_t configure(int mode, bool /*tma*/, int comp, int* per_sm)
+    {
+        if (mode == kModeStep) {
+            switch (comp) {
+            case kCompSum: return configure_flux_impl<float, kModeStepCons, false, kCompSum>(per_sm);
+            case kCompHiLo: return configure_flux_impl<float, kModeStepCons, false, kCompHiLo>(per_sm);
+            default: return configure_flux_impl<float, kModeStepCons, false, kCompNone>(per_sm);
+            }
+        }
+        return configure_flux_impl<float, kModeGodunov, false, kCompNone>(per_sm);
+    }
+    static cudaError_t launch(FluxParams<float> const& p, TmaMaps const* /*maps*/, int mode, int comp, int sms,
+                              cudaStream_t s)
+    {
+        if (mode == kModeStep) {
+            switch (comp) {
+            case kCompSum: return launch_flux_impl<float, kModeStepCons, false, kCompSum>(p, TmaMaps{}, sms, s);
+            case kCompHiLo: return launch_flux_impl<float, kModeStepCons, false, kCompHiLo>(p, TmaMaps{}, sms, s);
+            default: return launch_flux_impl<float, kModeStepCons, false, kCompNone>(p, TmaMaps{}, sms, s);
+            }
+        }
+        return launch_flux_impl<float, kModeGodunov, false, kCompNone>(p, TmaMaps{}, sms, s);
+    }
+};
+
+template <class T>
+cudaError_t configure_flux(int mode, bool tma, int comp, int* per_sm)
+{
+    return FluxDispatch<T>::configure(mode, tma, comp, per_sm);
 }
 
 template <class T>
-cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int sms, cudaStream_t s)
+cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int comp, int sms, cudaStream_t s)
 {
-    if (mode == kModeStep) {
-        if (maps != nullptr) {
-            return launch_flux_impl<T, kModeStep, true>(p, *maps, sms, s);
-        }
-        return launch_flux_impl<T, kModeStep, false>(p, TmaMaps{}, sms, s);
-    }
-    return launch_flux_impl<T, kModeGodunov, false>(p, TmaMaps{}, sms, s);
+    return FluxDispatch<T>::launch(p, maps, mode, comp, sms, s);
 }
 
 template <class T>
@@ -714,10 +854,10 @@ cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t
 int flux_tile_x() { return kTX; }
 int flux_tile_y() { return kTY; }
 
-template cudaError_t configure_flux<double>(int, bool, int*);
-template cudaError_t configure_flux<float>(int, bool, int*);
-template cudaError_t launch_flux<double>(FluxParams<double>, TmaMaps const*, int, int, cudaStream_t);
-template cudaError_t launch_flux<float>(FluxParams<float>, TmaMaps const*, int, int, cudaStream_t);
+template cudaError_t configure_flux<double>(int, bool, int, int*);
+template cudaError_t configure_flux<float>(int, bool, int, int*);
+template cudaError_t launch_flux<double>(FluxParams<double>, TmaMaps const*, int, int, int, cudaStream_t);
+template cudaError_t launch_flux<float>(FluxParams<float>, TmaMaps const*, int, int, int, cudaStream_t);
 template cudaError_t launch_ghost_shell<double>(GhostParams<double>, int, cudaStream_t);
 template cudaError_t launch_ghost_shell<float>(GhostParams<float>, int, cudaStream_t);
 template cudaError_t launch_finalize_dt<double>(SimScalars*, double, int, cudaStream_t);

@@ -10,6 +10,12 @@ namespace eulr {
 
 constexpr int kModeGodunov = 0; // per-operator godunov: cons updated in place from prim
 constexpr int kModeStep = 1;    // fused step: ping-pong buffers, next-step CFL reduction
+constexpr int kModeStepCons = 2; // fused step whose state is cons only (FP32): prim rebuilt on chip
+
+// Update arithmetic of the fused FP32 step.
+constexpr int kCompNone = 0;  // plain: cons -= sum of the six face terms, FP32
+constexpr int kCompSum = 1;   // compensated: error-free sum of cons and the six terms, one rounding
+constexpr int kCompHiLo = 2;  // compensated with a stored low word: cons = hi + lo (double-float)
 
 // Device scalars of a simulation.
 struct SimScalars {
@@ -38,10 +44,12 @@ struct FluxParams {
     T* cs_out;           // step mode: sound speed of the new state (interior)
     T gamma, gm1, inv_gm1, half_gm1;
     T ds0, ds1, ds2;     // face areas dx1*dx2, dx2*dx0, dx0*dx1
-    T dv;                // cell volume
+    double dv;           // cell volume
     T dtodv;             // dt/dv when dt_dev is null
-    const T* dt_dev;     // if set: dt/dv = (cfl * *dt_dev) / dv
-    T cfl;
+    const double* dt_dev; // if set: dt/dv = (cfl * *dt_dev) / dv, evaluated in double
+    double cfl;
+    CBundle<T> lo_in;    // compensated FP32 state: low words of cons (comp == 2)
+    Bundle<T> lo_out;
     T invdx0, invdx1, invdx2;
     unsigned long long* wmax; // step mode: atomicMax of the next max invdt
     int* status;              // step mode: set to 1 on a non-physical cell
@@ -54,6 +62,9 @@ struct GhostParams {
     Geom g;
     CBundle<T> cons_in;
     Bundle<T> cons_out;
+    CBundle<T> lo_in; // low words of cons (compensated FP32 state), copied when set
+    Bundle<T> lo_out;
+    int comp;         // kComp* of a cons-only FP32 state (prim_out unset)
     Bundle<T> prim_out;
     T* cs_out;
     T gamma, gm1;
@@ -75,12 +86,16 @@ cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1
                              int sms, cudaStream_t s);
 template <class T>
 cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s);
+// max invdt over all cells of a cons-only FP32 state (compensated: FP64
+// internal energy for low-pressure cells)
+cudaError_t launch_invdt_max_cons(CBundle<float> cons, long long n, float gamma, float ix0, float ix1, float ix2,
+                                  int comp, unsigned long long* wmax, int sms, cudaStream_t s);
 
 template <class T>
-cudaError_t configure_flux(int mode, bool tma, int* per_sm);
-// maps != nullptr selects TMA staging (step mode only)
+cudaError_t configure_flux(int mode, bool tma, int comp, int* per_sm);
+// maps != nullptr selects TMA staging (step mode only); comp: kComp* (float step mode)
 template <class T>
-cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int sms, cudaStream_t s);
+cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int comp, int sms, cudaStream_t s);
 int flux_tile_x();
 int flux_tile_y();
 template <class T>
@@ -89,6 +104,11 @@ template <class T>
 cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s);
 
 cudaError_t launch_fma_probe(int kind, int blocks, int iters, float* sink, cudaStream_t s);
-cudaError_t launch_totals(CBundle<double> cons, Geom g, double* out5, int sms, cudaStream_t s);
+template <class T>
+cudaError_t launch_totals(CBundle<T> cons, CBundle<T> lo, Geom g, double* work, cudaStream_t s);
+cudaError_t launch_state_to_f32(CBundle<double> prim, CBundle<double> cons, Bundle<float> hi, Bundle<float> lo,
+                                long long n, double gamma, int fp32_cons, int sms, cudaStream_t s);
+cudaError_t launch_state_from_f32(CBundle<float> hi, CBundle<float> lo, Bundle<double> prim, Bundle<double> cons,
+                                  long long n, double gamma, int sms, cudaStream_t s);
 
 } // namespace eulr

@@ -173,6 +173,41 @@ __global__ void __launch_bounds__(256) invdt_max_kernel(CBundle<T> prim, long lo
     }
 }
 
+// Max invdt over all cells of a cons-only FP32 state, with the pressure the
+// fused FP32 step uses (compensated states rescue low-pressure cells in FP64).
+__global__ void __launch_bounds__(256) invdt_max_cons_kernel(CBundle<float> cons, long long n, float gamma, float ix0,
+                                                             float ix1, float ix2, int comp, unsigned long long* wmax)
+{
+    float local = 0.0f;
+    float const gm1 = gamma - 1.0f;
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        float const d = cons.f[0][c];
+        float const e = cons.f[1][c];
+        float const m0 = cons.f[2][c];
+        float const m1 = cons.f[3][c];
+        float const m2 = cons.f[4][c];
+        float const r = 1.0f / d;
+        float const pr = comp ? pressure_f32c(d, e, m0, m1, m2, r, gm1, nullptr)
+                              : gm1 * (e - (0.5f * r) * (m0 * m0 + m1 * m1 + m2 * m2));
+        float const v = cell_invdt_exact(d, pr, m0 * r, m1 * r, m2 * r, gamma, ix0, ix1, ix2);
+        local = (v > local) ? v : local;
+    }
+    __shared__ float warp_best[8];
+    local = warp_max(local);
+    if ((threadIdx.x & 31) == 0) {
+        warp_best[threadIdx.x >> 5] = local;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = warp_best[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            b = (warp_best[w] > b) ? warp_best[w] : b;
+        }
+        atomicMax(wmax, order_bits(b));
+    }
+}
+
 // Sound speed sqrt((gamma p)/d) of every cell (perfect_gas.hpp:15-18).
 template <class T>
 __global__ void __launch_bounds__(256) sound_speed_kernel(CBundle<T> prim, T* cs, long long n, T gamma)
@@ -236,6 +271,13 @@ template <class T>
 cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s)
 {
     sound_speed_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cs, n, gamma);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_invdt_max_cons(CBundle<float> cons, long long n, float gamma, float ix0, float ix1, float ix2,
+                                  int comp, unsigned long long* wmax, int sms, cudaStream_t s)
+{
+    invdt_max_cons_kernel<<<grid_for(n, sms), 256, 0, s>>>(cons, n, gamma, ix0, ix1, ix2, comp, wmax);
     return cudaGetLastError();
 }
 

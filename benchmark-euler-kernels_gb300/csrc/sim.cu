@@ -2,27 +2,39 @@
 // simulations/euler_simulation.cpp:56-68 advanced entirely on the GPU.
 //
 // State layout in HBM: one allocation holding two copies (ping-pong A/B) of
-// the 5 prim fields, the 5 cons fields and the sound speed, each field a
-// layout_left block of n0*n1*n2 values padded to 256 bytes, then the device
-// scalars (SimScalars) and the totals workspace.  One step reads copy `cur`
-// and writes copy `1-cur`:
+// the state, each field a layout_left block of n0*n1*n2 values padded to 256
+// bytes, then the device scalars (SimScalars) and the totals workspace.  The
+// FP64 state keeps prim (5 fields), cons (5) and the sound speed (1): on
+// GB300 the FP64 pipe, not HBM, bounds the step, so values that cost FP64
+// instructions are stored rather than recomputed.  The FP32 states keep cons
+// only (plus 5 low-word fields for EULR_PRECISION_F32C_HILO): their step is
+// bound by HBM, so prim and the sound speed are rebuilt on chip.  One step reads copy
+// `cur` and writes copy `1-cur`:
 //   ghost_shell  -- out ghosts: cons copied, prim = cons_to_prim(cons)
 //                   (the reference runs cons_to_prim over ghosts too)
 //   flux (step)  -- out interior: HLLC update + cons_to_prim + sound speed,
 //                   and the max wavespeed of the new state
-//   finalize_dt  -- dt of the new state, simulated time += cfl*dt
+//   finalize_dt  -- dt of the new state, simulated time += cfl*dt (FP64)
 // Two steps (A->B, B->A) are captured once into a CUDA graph and replayed.
+//
+// Precisions: EULR_PRECISION_F64 (FP64 state and arithmetic),
+// EULR_PRECISION_F32C (FP32 state, compensated update, FP64 only for the
+// internal energy of low-pressure cells; 4-byte state words),
+// EULR_PRECISION_F32C_HILO (the same with an FP32 low word per conservative
+// field, a double-float state) and EULR_PRECISION_F32 (plain FP32, the
+// reference's real_t = float).  The ABI stays FP64 at the boundary: FP32
+// states are converted on the device when loaded and read back.
 #include "euler_gb300.h"
 #include "kernels.h"
 
 #include <cudaTypedefs.h>
 
 #include <cmath>
-#include <mutex>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -66,6 +78,8 @@ int cfail(cudaError_t e, const char* what)
 
 struct eulr_sim {
     int precision = EULR_PRECISION_F64;
+    int comp = kCompNone; // FP32 update arithmetic (kComp*)
+    size_t esize = 8;     // bytes per state word
     int device = 0;
     int sms = 0;
     Geom g{};
@@ -73,20 +87,23 @@ struct eulr_sim {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     void* slab = nullptr;
-    double* prim[2][5] = {};
-    double* cons[2][5] = {};
-    double* cs[2] = {};
+    void* prim[2][5] = {};
+    void* cons[2][5] = {};
+    void* lo[2][5] = {}; // compensated FP32 state with stored low words
+    void* cs[2] = {};
     SimScalars* sc = nullptr;
     double* totals = nullptr;
     int cur = 0;
-    int per_sm = 1; // resident CTAs per SM of the step kernel
-    bool tma = false; // stage planes by TMA (row pitch a multiple of 16 bytes)
+    int per_sm = 1;       // resident CTAs per SM of the step kernel
+    bool tma = false;     // stage planes by TMA (FP64, row pitch a multiple of 16 bytes)
     TmaMaps maps[2] = {}; // descriptors of copy 0 and copy 1 as step input
     bool loaded = false;
     cudaGraphExec_t graph = nullptr;
 };
 
 namespace {
+
+bool is_f64(eulr_sim const* s) { return s->precision == EULR_PRECISION_F64; }
 
 int check_sim(eulr_sim* s)
 {
@@ -102,6 +119,26 @@ int check_sim(eulr_sim* s)
 }
 
 long long ncell(eulr_sim const* s) { return s->g.ncell(); }
+
+template <class T>
+Bundle<T> bundle_of(void* const* f)
+{
+    Bundle<T> b;
+    for (int i = 0; i < 5; ++i) {
+        b.f[i] = static_cast<T*>(f[i]);
+    }
+    return b;
+}
+
+template <class T>
+CBundle<T> cbundle_of(void* const* f)
+{
+    CBundle<T> b;
+    for (int i = 0; i < 5; ++i) {
+        b.f[i] = static_cast<const T*>(f[i]);
+    }
+    return b;
+}
 
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime
 // (no link-time dependency on libcuda).
@@ -124,7 +161,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 // 3D tensor (n0, n1, n2) of doubles, layout_left, box (TX+2, TY+2, 1).
 // Requires the row pitch n0*8 to be a multiple of 16 bytes and a 16-byte
 // aligned base (fields are 256-byte aligned in the simulation's allocation).
-bool encode_field_map(CUtensorMap* m, double* base, Geom const& g)
+bool encode_field_map(CUtensorMap* m, void* base, Geom const& g)
 {
     auto enc = tensor_map_encoder();
     if (enc == nullptr) {
@@ -142,17 +179,18 @@ bool encode_field_map(CUtensorMap* m, double* base, Geom const& g)
     return r == CUDA_SUCCESS;
 }
 
-// TMA staging needs 16-byte row and plane pitches; the descriptors of both
-// copies are built once.  On any failure the plain-load staging is used.
+// TMA staging (FP64 state) needs 16-byte row and plane pitches; the
+// descriptors of both copies are built once.  On any failure the plain-load
+// staging is used.
 void setup_tma(eulr_sim* s)
 {
     s->tma = false;
-    if ((static_cast<size_t>(s->g.n0) * sizeof(double)) % 16 != 0) {
+    if (!is_f64(s) || (static_cast<size_t>(s->g.n0) * sizeof(double)) % 16 != 0) {
         return;
     }
     for (int c = 0; c < 2; ++c) {
-        double* f[7] = {s->prim[c][0], s->prim[c][1], s->prim[c][2], s->prim[c][3], s->prim[c][4], s->cs[c],
-                        s->cons[c][1]};
+        void* f[7] = {s->prim[c][0], s->prim[c][1], s->prim[c][2], s->prim[c][3], s->prim[c][4], s->cs[c],
+                      s->cons[c][1]};
         for (int i = 0; i < 7; ++i) {
             if (!encode_field_map(&s->maps[c].m[i], f[i], s->g)) {
                 return;
@@ -164,19 +202,31 @@ void setup_tma(eulr_sim* s)
 
 // One fused step from copy `in` to copy `1-in`; with `ev` (4 events) the
 // launches are bracketed for per-kernel timing.
-int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
+template <class T>
+int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
 {
     int const out = 1 - in;
-    double const ix0 = 1.0 / s->dx[0], ix1 = 1.0 / s->dx[1], ix2 = 1.0 / s->dx[2];
+    T const ix0 = T(1) / static_cast<T>(s->dx[0]);
+    T const ix1 = T(1) / static_cast<T>(s->dx[1]);
+    T const ix2 = T(1) / static_cast<T>(s->dx[2]);
+    T const gamma = static_cast<T>(s->gamma);
+    bool const has_lo = s->comp == kCompHiLo;
 
-    GhostParams<double> gp{};
+    GhostParams<T> gp{};
     gp.g = s->g;
-    std::memcpy(gp.cons_in.f, s->cons[in], sizeof(gp.cons_in.f));
-    std::memcpy(gp.cons_out.f, s->cons[out], sizeof(gp.cons_out.f));
-    std::memcpy(gp.prim_out.f, s->prim[out], sizeof(gp.prim_out.f));
-    gp.cs_out = s->cs[out];
-    gp.gamma = s->gamma;
-    gp.gm1 = s->gamma - 1.0;
+    gp.cons_in = cbundle_of<T>(s->cons[in]);
+    gp.cons_out = bundle_of<T>(s->cons[out]);
+    if (has_lo) {
+        gp.lo_in = cbundle_of<T>(s->lo[in]);
+        gp.lo_out = bundle_of<T>(s->lo[out]);
+    }
+    if (is_f64(s)) {
+        gp.prim_out = bundle_of<T>(s->prim[out]);
+        gp.cs_out = static_cast<T*>(s->cs[out]);
+    }
+    gp.comp = s->comp;
+    gp.gamma = gamma;
+    gp.gm1 = gamma - T(1);
     gp.invdx0 = ix0;
     gp.invdx1 = ix1;
     gp.invdx2 = ix2;
@@ -184,23 +234,29 @@ int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[0], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_ghost_shell<double>(gp, s->sms, s->stream), "ghost shell launch");
+    SIM_CUDA(launch_ghost_shell<T>(gp, s->sms, s->stream), "ghost shell launch");
 
-    FluxParams<double> p{};
+    FluxParams<T> p{};
     p.g = s->g;
-    std::memcpy(p.prim.f, s->prim[in], sizeof(p.prim.f));
-    p.cs = s->cs[in];
-    std::memcpy(p.cons_in.f, s->cons[in], sizeof(p.cons_in.f));
-    std::memcpy(p.cons_out.f, s->cons[out], sizeof(p.cons_out.f));
-    std::memcpy(p.prim_out.f, s->prim[out], sizeof(p.prim_out.f));
-    p.cs_out = s->cs[out];
-    p.gamma = s->gamma;
-    p.gm1 = s->gamma - 1.0;
-    p.inv_gm1 = 1.0 / (s->gamma - 1.0);
-    p.half_gm1 = 0.5 * (s->gamma - 1.0);
-    p.ds0 = s->dx[1] * s->dx[2];
-    p.ds1 = s->dx[2] * s->dx[0];
-    p.ds2 = s->dx[0] * s->dx[1];
+    if (is_f64(s)) {
+        p.prim = cbundle_of<T>(s->prim[in]);
+        p.cs = static_cast<const T*>(s->cs[in]);
+        p.prim_out = bundle_of<T>(s->prim[out]);
+        p.cs_out = static_cast<T*>(s->cs[out]);
+    }
+    p.cons_in = cbundle_of<T>(s->cons[in]);
+    p.cons_out = bundle_of<T>(s->cons[out]);
+    if (has_lo) {
+        p.lo_in = cbundle_of<T>(s->lo[in]);
+        p.lo_out = bundle_of<T>(s->lo[out]);
+    }
+    p.gamma = gamma;
+    p.gm1 = gamma - T(1);
+    p.inv_gm1 = T(1) / (gamma - T(1));
+    p.half_gm1 = T(0.5) * (gamma - T(1));
+    p.ds0 = static_cast<T>(s->dx[1] * s->dx[2]);
+    p.ds1 = static_cast<T>(s->dx[2] * s->dx[0]);
+    p.ds2 = static_cast<T>(s->dx[0] * s->dx[1]);
     p.dv = s->dx[0] * s->dx[1] * s->dx[2];
     p.dt_dev = &s->sc->dt;
     p.cfl = s->cfl;
@@ -213,46 +269,131 @@ int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[1], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_flux<double>(p, s->tma ? &s->maps[in] : nullptr, kModeStep, s->sms, s->stream), "step launch");
+    SIM_CUDA(launch_flux<T>(p, s->tma ? &s->maps[in] : nullptr, kModeStep, s->comp, s->sms, s->stream), "step launch");
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[2], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_finalize_dt<double>(s->sc, s->cfl, 1, s->stream), "finalize launch");
+    SIM_CUDA(launch_finalize_dt<T>(s->sc, static_cast<T>(s->cfl), 1, s->stream), "finalize launch");
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[3], s->stream), "cudaEventRecord");
     }
     return EULR_SUCCESS;
 }
 
-// After a state was loaded into copy 0: sound speed, dt of the state, zeroed
-// clock and status.
+int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
+{
+    return is_f64(s) ? enqueue_step_t<double>(s, in, ev) : enqueue_step_t<float>(s, in, ev);
+}
+
+// After a state was loaded into copy 0: sound speed (FP64 state), dt of the
+// state, zeroed clock and status.
 int prepare_loaded(eulr_sim* s)
 {
     s->cur = 0;
-    CBundle<double> pv;
-    std::memcpy(pv.f, s->prim[0], sizeof(pv.f));
-    SIM_CUDA(launch_sound_speed<double>(pv, s->cs[0], ncell(s), s->gamma, s->sms, s->stream), "sound speed launch");
     SIM_CUDA(cudaMemsetAsync(s->sc, 0, sizeof(SimScalars), s->stream), "cudaMemsetAsync");
-    SIM_CUDA(launch_invdt_max<double>(pv, ncell(s), s->gamma, 1.0 / s->dx[0], 1.0 / s->dx[1], 1.0 / s->dx[2],
-                                      &s->sc->wmax, s->sms, s->stream),
-             "invdt launch");
-    SIM_CUDA(launch_finalize_dt<double>(s->sc, s->cfl, 0, s->stream), "finalize launch");
+    if (is_f64(s)) {
+        CBundle<double> pv = cbundle_of<double>(s->prim[0]);
+        SIM_CUDA(launch_sound_speed<double>(pv, static_cast<double*>(s->cs[0]), ncell(s), s->gamma, s->sms, s->stream),
+                 "sound speed launch");
+        SIM_CUDA(launch_invdt_max<double>(pv, ncell(s), s->gamma, 1.0 / s->dx[0], 1.0 / s->dx[1], 1.0 / s->dx[2],
+                                          &s->sc->wmax, s->sms, s->stream),
+                 "invdt launch");
+        SIM_CUDA(launch_finalize_dt<double>(s->sc, s->cfl, 0, s->stream), "finalize launch");
+    } else {
+        float const g = static_cast<float>(s->gamma);
+        SIM_CUDA(launch_invdt_max_cons(cbundle_of<float>(s->cons[0]), ncell(s), g, 1.0f / static_cast<float>(s->dx[0]),
+                                       1.0f / static_cast<float>(s->dx[1]), 1.0f / static_cast<float>(s->dx[2]),
+                                       s->comp != kCompNone ? 1 : 0, &s->sc->wmax, s->sms, s->stream),
+                 "invdt launch");
+        SIM_CUDA(launch_finalize_dt<float>(s->sc, static_cast<float>(s->cfl), 0, s->stream), "finalize launch");
+    }
     s->loaded = true;
     return EULR_SUCCESS;
 }
 
-template <class B>
-int copy_in(eulr_sim* s, double* const* dst, B const& src)
+// Temporary FP64 fields on the device for the FP32 states' conversions.
+struct Staging {
+    void* base = nullptr;
+    double* f[10] = {};
+    ~Staging()
+    {
+        if (base != nullptr) {
+            cudaFree(base);
+        }
+    }
+};
+
+int make_staging(eulr_sim* s, Staging& st, int nfields)
 {
-    const double* f[5];
-    std::memcpy(f, &src, sizeof(f));
+    size_t const field = pad256(static_cast<size_t>(ncell(s)) * sizeof(double));
+    SIM_CUDA(cudaMalloc(&st.base, field * nfields), "cudaMalloc(conversion staging)");
+    for (int i = 0; i < nfields; ++i) {
+        st.f[i] = reinterpret_cast<double*>(static_cast<char*>(st.base) + field * i);
+    }
+    return EULR_SUCCESS;
+}
+
+// Copy a user bundle (host or device) into device FP64 fields.
+int copy_in(eulr_sim* s, void* const* dst, const double* const* src)
+{
     size_t const bytes = static_cast<size_t>(ncell(s)) * sizeof(double);
     for (int i = 0; i < 5; ++i) {
-        if (f[i] == nullptr) {
+        if (src[i] == nullptr) {
             return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "state field is NULL");
         }
-        SIM_CUDA(cudaMemcpyAsync(dst[i], f[i], bytes, cudaMemcpyDefault, s->stream), "cudaMemcpyAsync(in)");
+        SIM_CUDA(cudaMemcpyAsync(dst[i], src[i], bytes, cudaMemcpyDefault, s->stream), "cudaMemcpyAsync(in)");
     }
+    return EULR_SUCCESS;
+}
+
+// Load FP64 prim (and cons, or nullptr to derive it) already on the device
+// into an FP32 state's copy 0.
+int load_f32(eulr_sim* s, double* const* prim64, double* const* cons64)
+{
+    CBundle<double> pv, cv;
+    for (int i = 0; i < 5; ++i) {
+        pv.f[i] = prim64[i];
+        cv.f[i] = cons64 != nullptr ? cons64[i] : nullptr;
+    }
+    Bundle<float> lo{};
+    if (s->comp == kCompHiLo) {
+        lo = bundle_of<float>(s->lo[0]);
+    }
+    SIM_CUDA(launch_state_to_f32(pv, cv, bundle_of<float>(s->cons[0]), lo, ncell(s), s->gamma,
+                                 s->precision == EULR_PRECISION_F32 ? 1 : 0, s->sms, s->stream),
+             "state conversion");
+    return EULR_SUCCESS;
+}
+
+int set_state_impl(eulr_sim* s, const double* const* prim, const double* const* cons)
+{
+    if (is_f64(s)) {
+        SIM_TRY(copy_in(s, s->prim[0], prim));
+        if (cons != nullptr) {
+            SIM_TRY(copy_in(s, s->cons[0], cons));
+        } else {
+            double const gm1 = s->gamma - 1.0;
+            SIM_CUDA(launch_prim_to_cons<double>(cbundle_of<double>(s->prim[0]), bundle_of<double>(s->cons[0]),
+                                                 ncell(s), gm1, 1.0 / gm1, s->sms, s->stream),
+                     "prim_to_cons");
+        }
+        return prepare_loaded(s);
+    }
+    Staging st;
+    SIM_TRY(make_staging(s, st, cons != nullptr ? 10 : 5));
+    void* pd[5];
+    void* cd[5];
+    for (int i = 0; i < 5; ++i) {
+        pd[i] = st.f[i];
+        cd[i] = st.f[5 + i];
+    }
+    SIM_TRY(copy_in(s, pd, prim));
+    if (cons != nullptr) {
+        SIM_TRY(copy_in(s, cd, cons));
+    }
+    SIM_TRY(load_f32(s, st.f, cons != nullptr ? st.f + 5 : nullptr));
+    SIM_TRY(prepare_loaded(s));
+    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize"); // staging is freed next
     return EULR_SUCCESS;
 }
 
@@ -267,8 +408,9 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
         return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "out is NULL");
     }
     *out = nullptr;
-    if (precision != EULR_PRECISION_F64) {
-        return eulr::sim_fail(EULR_ERR_UNSUPPORTED, "only EULR_PRECISION_F64 is available in this build");
+    if (precision != EULR_PRECISION_F64 && precision != EULR_PRECISION_F32C && precision != EULR_PRECISION_F32 &&
+        precision != EULR_PRECISION_F32C_HILO) {
+        return eulr::sim_fail(EULR_ERR_UNSUPPORTED, "unknown precision");
     }
     if (n0 < 1 || n1 < 1 || n2 < 1) {
         return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "grid extents must be >= 1");
@@ -290,6 +432,10 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
         return eulr::sim_fail(EULR_ERR_OUT_OF_MEMORY, "host allocation failed");
     }
     s->precision = precision;
+    s->esize = precision == EULR_PRECISION_F64 ? sizeof(double) : sizeof(float);
+    s->comp = precision == EULR_PRECISION_F32C       ? kCompSum
+              : precision == EULR_PRECISION_F32C_HILO ? kCompHiLo
+                                                       : kCompNone;
     s->g = make_geom(n0, n1, n2);
     s->gamma = gamma;
     s->dx[0] = dx0;
@@ -317,32 +463,43 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
         }
         s->own_stream = true;
     }
-    size_t const field = pad256(static_cast<size_t>(ncell(s)) * sizeof(double));
+    size_t const field = pad256(static_cast<size_t>(ncell(s)) * s->esize);
     size_t const scal = pad256(sizeof(SimScalars));
     size_t const tot = pad256(kTotalsWork * sizeof(double));
-    size_t const bytes = 22 * field + scal + tot;
+    // FP64: prim + cons + sound speed per copy; FP32: cons (+ low words) only
+    int const per_copy = is_f64(s) ? 11 : (s->comp == kCompHiLo ? 10 : 5);
+    size_t const bytes = 2 * per_copy * field + scal + tot;
     e = cudaMalloc(&s->slab, bytes);
     if (e != cudaSuccess) {
         return bail(cfail(e, "cudaMalloc(simulation state)"));
     }
     char* b = static_cast<char*>(s->slab);
     for (int c = 0; c < 2; ++c) {
-        for (int f = 0; f < 5; ++f) {
-            s->prim[c][f] = reinterpret_cast<double*>(b);
+        if (is_f64(s)) {
+            for (int f = 0; f < 5; ++f) {
+                s->prim[c][f] = b;
+                b += field;
+            }
+            s->cs[c] = b;
             b += field;
         }
         for (int f = 0; f < 5; ++f) {
-            s->cons[c][f] = reinterpret_cast<double*>(b);
+            s->cons[c][f] = b;
             b += field;
         }
-        s->cs[c] = reinterpret_cast<double*>(b);
-        b += field;
+        if (s->comp == kCompHiLo) {
+            for (int f = 0; f < 5; ++f) {
+                s->lo[c][f] = b;
+                b += field;
+            }
+        }
     }
     s->sc = reinterpret_cast<SimScalars*>(b);
     b += scal;
     s->totals = reinterpret_cast<double*>(b);
     setup_tma(s);
-    e = configure_flux<double>(kModeStep, s->tma, &s->per_sm);
+    e = is_f64(s) ? configure_flux<double>(kModeStep, s->tma, kCompNone, &s->per_sm)
+                  : configure_flux<float>(kModeStep, false, s->comp, &s->per_sm);
     if (e != cudaSuccess) {
         return bail(cfail(e, "step kernel configure"));
     }
@@ -386,37 +543,43 @@ int eulr_sim_destroy(eulr_sim* s)
 int eulr_sim_set_prim_f64(eulr_sim* s, eulr_prim_cf64 prim)
 {
     SIM_TRY(check_sim(s));
-    SIM_TRY(copy_in(s, s->prim[0], prim));
-    CBundle<double> pv;
-    Bundle<double> cv;
-    std::memcpy(pv.f, s->prim[0], sizeof(pv.f));
-    std::memcpy(cv.f, s->cons[0], sizeof(cv.f));
-    double const gm1 = s->gamma - 1.0;
-    SIM_CUDA(launch_prim_to_cons<double>(pv, cv, ncell(s), gm1, 1.0 / gm1, s->sms, s->stream), "prim_to_cons");
-    return prepare_loaded(s);
+    const double* p[5] = {prim.d, prim.p, prim.ux0, prim.ux1, prim.ux2};
+    return set_state_impl(s, p, nullptr);
 }
 
 int eulr_sim_set_state_f64(eulr_sim* s, eulr_prim_cf64 prim, eulr_cons_cf64 cons)
 {
     SIM_TRY(check_sim(s));
-    SIM_TRY(copy_in(s, s->prim[0], prim));
-    SIM_TRY(copy_in(s, s->cons[0], cons));
-    return prepare_loaded(s);
+    const double* p[5] = {prim.d, prim.p, prim.ux0, prim.ux1, prim.ux2};
+    const double* c[5] = {cons.d, cons.e, cons.mx0, cons.mx1, cons.mx2};
+    return set_state_impl(s, p, c);
 }
 
 int eulr_sim_init_implode(eulr_sim* s)
 {
     SIM_TRY(check_sim(s));
+    if (is_f64(s)) {
+        SIM_CUDA(launch_init_implode<double>(bundle_of<double>(s->prim[0]), s->g, s->dx[0], s->dx[1], s->dx[2], s->sms,
+                                             s->stream),
+                 "init_implode");
+        double const gm1 = s->gamma - 1.0;
+        SIM_CUDA(launch_prim_to_cons<double>(cbundle_of<double>(s->prim[0]), bundle_of<double>(s->cons[0]), ncell(s),
+                                             gm1, 1.0 / gm1, s->sms, s->stream),
+                 "prim_to_cons");
+        return prepare_loaded(s);
+    }
+    // FP32 states: the FP64 implosion state, converted on the device
+    Staging st;
+    SIM_TRY(make_staging(s, st, 5));
     Bundle<double> pw;
-    CBundle<double> pv;
-    Bundle<double> cv;
-    std::memcpy(pw.f, s->prim[0], sizeof(pw.f));
-    std::memcpy(pv.f, s->prim[0], sizeof(pv.f));
-    std::memcpy(cv.f, s->cons[0], sizeof(cv.f));
+    for (int i = 0; i < 5; ++i) {
+        pw.f[i] = st.f[i];
+    }
     SIM_CUDA(launch_init_implode<double>(pw, s->g, s->dx[0], s->dx[1], s->dx[2], s->sms, s->stream), "init_implode");
-    double const gm1 = s->gamma - 1.0;
-    SIM_CUDA(launch_prim_to_cons<double>(pv, cv, ncell(s), gm1, 1.0 / gm1, s->sms, s->stream), "prim_to_cons");
-    return prepare_loaded(s);
+    SIM_TRY(load_f32(s, st.f, nullptr));
+    SIM_TRY(prepare_loaded(s));
+    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    return EULR_SUCCESS;
 }
 
 int eulr_sim_advance(eulr_sim* s, int nsteps)
@@ -466,19 +629,43 @@ int eulr_sim_get_state_f64(eulr_sim* s, eulr_prim_f64 prim, eulr_cons_f64 cons)
 {
     SIM_TRY(check_sim(s));
     size_t const bytes = static_cast<size_t>(ncell(s)) * sizeof(double);
-    double* pf[5];
-    double* cf[5];
-    std::memcpy(pf, &prim, sizeof(pf));
-    std::memcpy(cf, &cons, sizeof(cf));
+    double* pf[5] = {prim.d, prim.p, prim.ux0, prim.ux1, prim.ux2};
+    double* cf[5] = {cons.d, cons.e, cons.mx0, cons.mx1, cons.mx2};
+    if (is_f64(s)) {
+        for (int i = 0; i < 5; ++i) {
+            if (pf[i] != nullptr) {
+                SIM_CUDA(cudaMemcpyAsync(pf[i], s->prim[s->cur][i], bytes, cudaMemcpyDefault, s->stream), "copy out");
+            }
+            if (cf[i] != nullptr) {
+                SIM_CUDA(cudaMemcpyAsync(cf[i], s->cons[s->cur][i], bytes, cudaMemcpyDefault, s->stream), "copy out");
+            }
+        }
+        SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+        return EULR_SUCCESS;
+    }
+    Staging st;
+    SIM_TRY(make_staging(s, st, 10));
+    Bundle<double> pw, cw;
+    for (int i = 0; i < 5; ++i) {
+        pw.f[i] = st.f[i];
+        cw.f[i] = st.f[5 + i];
+    }
+    CBundle<float> lo{};
+    if (s->comp == kCompHiLo) {
+        lo = cbundle_of<float>(s->lo[s->cur]);
+    }
+    SIM_CUDA(launch_state_from_f32(cbundle_of<float>(s->cons[s->cur]), lo, pw, cw, ncell(s), s->gamma, s->sms,
+                                   s->stream),
+             "state conversion");
     for (int i = 0; i < 5; ++i) {
         if (pf[i] != nullptr) {
-            SIM_CUDA(cudaMemcpyAsync(pf[i], s->prim[s->cur][i], bytes, cudaMemcpyDefault, s->stream), "copy out");
+            SIM_CUDA(cudaMemcpyAsync(pf[i], pw.f[i], bytes, cudaMemcpyDefault, s->stream), "copy out");
         }
         if (cf[i] != nullptr) {
-            SIM_CUDA(cudaMemcpyAsync(cf[i], s->cons[s->cur][i], bytes, cudaMemcpyDefault, s->stream), "copy out");
+            SIM_CUDA(cudaMemcpyAsync(cf[i], cw.f[i], bytes, cudaMemcpyDefault, s->stream), "copy out");
         }
     }
-    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize"); // staging is freed next
     return EULR_SUCCESS;
 }
 
@@ -506,6 +693,9 @@ int eulr_sim_status(eulr_sim* s)
     SimScalars h{};
     SIM_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(h), cudaMemcpyDeviceToHost, s->stream), "copy scalars");
     SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    if (h.status & 2) {
+        return eulr::sim_fail(EULR_ERR_CUDA, "a staged plane never arrived (a bounded wait ran out)");
+    }
     if (h.status != 0) {
         return eulr::sim_fail(EULR_ERR_NONFINITE, "a cell became non-finite or non-physical");
     }
@@ -554,12 +744,35 @@ int eulr_sim_totals(eulr_sim* s, double out[5])
     if (out == nullptr) {
         return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "out is NULL");
     }
-    CBundle<double> cv;
-    std::memcpy(cv.f, s->cons[s->cur], sizeof(cv.f));
-    SIM_CUDA(launch_totals(cv, s->g, s->totals, s->sms, s->stream), "totals launch");
+    if (is_f64(s)) {
+        SIM_CUDA(launch_totals<double>(cbundle_of<double>(s->cons[s->cur]), CBundle<double>{}, s->g, s->totals,
+                                       s->stream),
+                 "totals launch");
+    } else {
+        CBundle<float> lo{};
+        if (s->comp == kCompHiLo) {
+            lo = cbundle_of<float>(s->lo[s->cur]);
+        }
+        SIM_CUDA(launch_totals<float>(cbundle_of<float>(s->cons[s->cur]), lo, s->g, s->totals, s->stream),
+                 "totals launch");
+    }
     SIM_CUDA(cudaMemcpyAsync(out, s->totals + 256 * 5, 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream),
              "copy totals");
     SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    return EULR_SUCCESS;
+}
+
+int eulr_sim_state_bytes(eulr_sim* s, long long* bytes_per_step)
+{
+    SIM_TRY(check_sim(s));
+    if (bytes_per_step == nullptr) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "bytes_per_step is NULL");
+    }
+    // conservative words read and written once per interior cell
+    long long const words = (s->comp == kCompHiLo ? 10 : 5);
+    long long const ix = s->g.n0 > 2 ? s->g.n0 - 2 : 0, iy = s->g.n1 > 2 ? s->g.n1 - 2 : 0,
+                    iz = s->g.n2 > 2 ? s->g.n2 - 2 : 0;
+    *bytes_per_step = 2 * words * static_cast<long long>(s->esize) * ix * iy * iz;
     return EULR_SUCCESS;
 }
 

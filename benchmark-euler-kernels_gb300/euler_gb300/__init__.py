@@ -24,7 +24,7 @@ STATUS_NAMES = {
     -6: "EULR_ERR_TOO_LARGE", -7: "EULR_ERR_NONFINITE", -8: "EULR_ERR_NO_DEVICE",
     -9: "EULR_ERR_UNSUPPORTED",
 }
-PRECISION = {"f64": 0, "f32c": 1, "f32": 2}
+PRECISION = {"f64": 0, "f32c": 1, "f32": 2, "f32c_hilo": 3}
 
 
 class EulerError(RuntimeError):
@@ -71,6 +71,7 @@ _SIGNATURES = [
     ("eulr_sim_launches_per_step", _I, [_P]),
     ("eulr_sim_profile_step", _I, [_P, ctypes.POINTER(_F)]),
     ("eulr_sim_totals", _I, [_P, ctypes.POINTER(_D)]),
+    ("eulr_sim_state_bytes", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("eulr_probe_fma_rate", _I, [_I, _I, ctypes.POINTER(_D)]),
 ]
 
@@ -287,6 +288,11 @@ class Simulation:
         out = (ctypes.c_double * 5)()
         check(load().eulr_sim_totals(self._h, out))
         return list(out)
+
+    def state_bytes(self) -> int:
+        out = ctypes.c_longlong()
+        check(load().eulr_sim_state_bytes(self._h, ctypes.byref(out)))
+        return out.value
 
 
 def fma_rate(kind: str = "f64", iters: int = 20000) -> float:

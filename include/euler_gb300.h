@@ -205,9 +205,13 @@ int eulr_godunov_devdt_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int 
 typedef struct eulr_sim eulr_sim;
 
 typedef enum eulr_precision {
-    EULR_PRECISION_F64 = 0,  /* plain FP64 */
-    EULR_PRECISION_F32C = 1, /* FP32 state with compensated update */
-    EULR_PRECISION_F32 = 2   /* plain FP32 (real_t = float) */
+    EULR_PRECISION_F64 = 0,      /* plain FP64 */
+    EULR_PRECISION_F32C = 1,     /* FP32 state (4-byte words), FP32 fluxes, compensated update: the cell
+                                    and its six face terms are summed with error-free transformations and
+                                    rounded once; FP64 only for the internal energy of low-pressure cells */
+    EULR_PRECISION_F32 = 2,      /* plain FP32 (the reference's real_t = float) */
+    EULR_PRECISION_F32C_HILO = 3 /* EULR_PRECISION_F32C with an FP32 low word per conservative field
+                                    (double-float state, 8-byte words) */
 } eulr_precision;
 
 int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double dx0, double dx1, double dx2,
@@ -250,6 +254,11 @@ int eulr_sim_profile_step(eulr_sim* sim, float ms[3]);
 /* Conservation totals: sum over interior cells of (d, e, mx0, mx1, mx2),
  * accumulated in FP64 on the device; waits for the stream. */
 int eulr_sim_totals(eulr_sim* sim, double out[5]);
+
+/* Algorithmic HBM bytes of one step: the conservative state read and written
+ * once per interior cell (5 words, or 10 with stored low words, of the
+ * state's word size). */
+int eulr_sim_state_bytes(eulr_sim* sim, long long* bytes_per_step);
 
 /* ------------------------------------------------------------ measurement */
 
