@@ -20,6 +20,10 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libeuler_gb300.so")
+APPS_DIR = os.path.join(PKG_ROOT, "apps")
+APPS = ("euler_simulation", "euler_benchmarks")
+APP_INCLUDES = ["-I", INCLUDE, "-I", os.path.join(INCLUDE, "euler_operators"),
+                "-I", os.path.join(INCLUDE, "euler_operators_kokkos")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC] + ARCH
@@ -65,7 +69,24 @@ def build(verbose: bool = False, force: bool = False) -> str:
         list(ex.map(run, jobs))
     if jobs or force or _stale(LIB_PATH, objs):
         run([nvcc, "-shared", *ARCH, "-o", LIB_PATH, *objs])
+    # host applications over the drop-in headers, linked against the library
+    app_headers = headers + sorted(glob.glob(os.path.join(INCLUDE, "euler_operators", "*.hpp")) +
+                                   glob.glob(os.path.join(INCLUDE, "euler_operators_kokkos", "*.hpp")))
+    app_jobs = []
+    for app in APPS:
+        src = os.path.join(APPS_DIR, app + ".cpp")
+        exe = os.path.join(LIB_DIR, app)
+        if force or _stale(exe, [src, LIB_PATH] + app_headers):
+            app_jobs.append([nvcc, "-std=c++20", "-O2", *APP_INCLUDES, src, "-o", exe, "-L", LIB_DIR, "-leuler_gb300",
+                             "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(app_jobs))) as ex:
+        list(ex.map(run, app_jobs))
     return LIB_PATH
+
+
+def app_path(name: str) -> str:
+    """Path of a built host application (euler_simulation, euler_benchmarks)."""
+    return os.path.join(LIB_DIR, name)
 
 
 if __name__ == "__main__":

@@ -12,6 +12,7 @@ Usage (from the repository root):  python tests/golden/make_golden.py
 from __future__ import annotations
 
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -89,6 +90,9 @@ def main():
         operator_case(f"ops_2x5x4_{tag}", 2, 5, 4, (0.5, 0.25, 1 / 3), seed=14, dtype=dtype)
         uniform_case(f"uniform_10_{tag}", 10, dtype)
         implode_case(f"implode_16_{tag}", 16, (1, 10), dtype)
+    # NPY files written by the reference's own writer (simulations/save_npy.cpp)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "npy"], check=True)
+    subprocess.run([os.path.join(ROOT, "oracle", "_ref", "npy_golden"), OUT], check=True)
     print("golden fixtures written to", OUT)
 
 
