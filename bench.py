@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--no-ops", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-fp32c", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-grids", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=200)
     ap.add_argument("--precision-study", action="store_true",
                     help="implosion, FP32 states vs the plain FP64 run (L1/Linf of rho, p, |u|); prints its own JSON")
     ap.add_argument("--study-n", type=int, nargs="+", default=[512, 768])
@@ -318,6 +321,50 @@ def run_precision_study(args):
     return 0
 
 
+def draw_batch(ngrids, seed=0):
+    """The batched workload: each axis length drawn from {24,32,48,64,96,128}
+    (interior cells; dx = 1/n per axis), gamma U[1.1, 1.67], inner/outer
+    pressure ratio log-U[0.01, 1], density ratio log-U[0.05, 1], step on
+    x + y + z < c with c U[0.1, 0.5] (numpy PCG64)."""
+    import numpy as np
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    grids, ics = [], []
+    for _ in range(ngrids):
+        n = [int(rng.choice((24, 32, 48, 64, 96, 128))) for _ in range(3)]
+        gamma = float(rng.uniform(1.1, 1.67))
+        pr = float(np.exp(rng.uniform(np.log(0.01), 0.0)))
+        rr = float(np.exp(rng.uniform(np.log(0.05), 0.0)))
+        c = float(rng.uniform(0.1, 0.5))
+        grids.append((n[0] + 2, n[1] + 2, n[2] + 2, gamma, 1.0 / n[0], 1.0 / n[1], 1.0 / n[2]))
+        ics.append((c, rr, pr))
+    return grids, ics
+
+
+def run_batch_leg(torch, E, stream, args, precision):
+    """All grids of the batched workload advanced together (one persistent
+    launch per step), autotuned tile shape and chunk length."""
+    grids, ics = draw_batch(args.batch_grids, seed=0)
+    with E.Batch(grids, cfl=CFL, precision=precision, stream=stream) as bt:
+        for g, (c, rr, pr) in enumerate(ics):
+            bt.init_step(g, c, rr, pr)
+        tune = bt.autotune(trial_steps=2)
+        info = bt.info()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        bt.advance(args.batch_steps)
+        e.record(stream)
+        e.synchronize()
+        ms = s.elapsed_time(e)
+        status = bt.status()
+        t0 = bt.time(0)
+    return {"value": info["interior_cells"] * args.batch_steps / (ms * 1e-3) / 1e9, "unit": UNIT,
+            "grids": len(grids), "steps": args.batch_steps, "interior_cells": info["interior_cells"],
+            "ms_per_step": ms / args.batch_steps, "work_items": info["items"], "autotune": tune, "status": status,
+            "grid0_t": t0[0]}
+
+
 def time_ops(torch, E, prim, n_int):
     """Each reference operator alone, one call after warm-up (CUDA events)."""
     n0 = n_int + 2
@@ -461,6 +508,11 @@ def run_ours(args):
         del ref
         torch.cuda.empty_cache()
 
+    batch = None
+    if not args.no_batch:
+        batch = {p: run_batch_leg(torch, E, stream, args, p) for p in ("f64", "f32c")}
+        torch.cuda.empty_cache()
+
     ops = None
     if not args.no_ops and rank == 0:
         prim = random_prim_device(torch, n0, n0, n0, seed=1)
@@ -518,6 +570,7 @@ def run_ours(args):
             "e2e": e2e,
             "cpu_baseline": cpu,
             "fp32c": fp32c,
+            "batch": batch,
             "operators": ops,
             "status": status,
             "sim": {"t": t_sim, "steps_taken": nsteps},

@@ -40,6 +40,7 @@
 #include <ctime>
 #include <fstream>
 #include <functional>
+#include <iomanip>
 #include <iostream>
 #include <sstream>
 #include <string>
@@ -235,6 +236,7 @@ void write_json(std::ostream& os, std::vector<Result> const& rs, std::string con
     cudaGetDevice(&dev);
     cudaDeviceProp prop {};
     cudaGetDeviceProperties(&prop, dev);
+    os.precision(17);
     os << "{\n  \"context\": {\n"
        << "    \"date\": \"" << date << "\",\n"
        << "    \"host_name\": \"" << json_escape(host) << "\",\n"

@@ -263,301 +263,392 @@ __device__ __forceinline__ void compensated_add(float& sum, float& err, float k,
 }
 __device__ __forceinline__ void compensated_add(double&, double&, double, double) {}
 
+// Per-CTA state of the tile engine that lives across work items.
+template <class T>
+struct TileCtx {
+    unsigned long long* bars; // one mbarrier per slot (TMA ring)
+    T* smem;                  // plane slots
+    T* fx;                    // x-face fluxes (5 fields)
+    T* fy;                    // y-face fluxes
+    T* fz;                    // z-face fluxes
+    unsigned phase;           // bit s: parity of slot s's next completion (TMA ring)
+    unsigned inflight;        // bit s: a TMA into slot s has not been waited for
+    bool timed_out;           // a bounded mbarrier wait ran out
+    long long wkey;           // ordered bits of this thread's max wavespeed
+    bool bad;                 // this thread saw a non-physical cell
+};
+
+template <class T, int NSLOT>
+__device__ __forceinline__ bool wait_slot(TileCtx<T>& c, int s)
+{
+    bool const ok = mbar_wait(&c.bars[s], (c.phase >> s) & 1u);
+    c.phase ^= 1u << s;
+    c.inflight &= ~(1u << s);
+    return ok;
+}
+
+// One work item: interior planes [kb, ke) of the TX x TY column whose first
+// cell is (1 + tx*TX, 1 + ty*TY), with update coefficients k0..k2 (dt/dv
+// times the face areas).  Returns false when a staged plane never arrived.
+template <class T, int TX, int TY, int NSLOT, int MODE, bool TMA, int COMP>
+__device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p, TmaMaps const& maps, T k0, T k1,
+                                          T k2, int tx, int ty, int kc)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    int const tid = threadIdx.x;
+    int const ti = tid % TX;
+    int const tj = tid / TX;
+    int const center = (tj + 1) * L::HX + ti + 1;
+    T* const smem = c.smem;
+    T* const fx = c.fx;
+    T* const fy = c.fy;
+    T* const fz = c.fz;
+
+    int const i0 = 1 + tx * TX;
+    int const j0 = 1 + ty * TY;
+    int const kb = 1 + kc * p.kchunk;
+    int const ke = min(kb + p.kchunk, p.g.n2 - 1);
+    int const i = i0 + ti;
+    int const j = j0 + tj;
+    bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
+
+    __syncthreads(); // the previous item's readers of slots and fluxes are done
+    if (TMA) {
+        // planes kb-1, kb, kb+1 -> slots 0, 1, 2 (kb+1 <= ke always)
+        if (tid == 0) {
+            issue_plane<T, TX, TY, NSLOT>(smem, c.bars, 0, maps, i0, j0, kb - 1);
+            issue_plane<T, TX, TY, NSLOT>(smem, c.bars, 1, maps, i0, j0, kb);
+            issue_plane<T, TX, TY, NSLOT>(smem, c.bars, 2, maps, i0, j0, kb + 1);
+        }
+        c.inflight |= 7u;
+        c.timed_out |= !wait_slot<T, NSLOT>(c, 0);
+        c.timed_out |= !wait_slot<T, NSLOT>(c, 1);
+    } else {
+        load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, 0, p, i0, j0, kb - 1);
+        load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, 1, p, i0, j0, kb);
+        __syncthreads();
+    }
+    // z face below the chunk's first plane, kept in registers in global
+    // axes (the z face frame has n = mx2, t1 = mx0, t2 = mx1)
+    T zlo[5];
+    {
+        Flux<T> const f0 = hllc_flux(load_side<T, L::PLANE_PAD>(slot_field<T, TX, TY, NSLOT>(smem, 0, 0), center, 2),
+                                     load_side<T, L::PLANE_PAD>(slot_field<T, TX, TY, NSLOT>(smem, 1, 0), center, 2));
+        zlo[0] = f0.d;
+        zlo[1] = f0.e;
+        zlo[2] = f0.t1;
+        zlo[3] = f0.t2;
+        zlo[4] = f0.n;
+    }
+    if (__syncthreads_or(c.timed_out)) { // slot 0 is refilled next
+        return false;
+    }
+    if (TMA) {
+        if (kb + 2 <= ke) {
+            if (tid == 0) {
+                issue_plane<T, TX, TY, NSLOT>(smem, c.bars, 0, maps, i0, j0, kb + 2);
+            }
+            c.inflight |= 1u;
+        }
+    }
+
+    for (int k = kb; k < ke; ++k) {
+        int const cur = (k - kb + 1) % NSLOT;
+        int const nxt = (k - kb + 2) % NSLOT;
+        // this cell's conservative state, fetched while the faces are solved
+        T u[5];
+        T ulo[5] = {T(0), T(0), T(0), T(0), T(0)};
+        long long const o = p.g.at(i, j, k);
+        if (own) {
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                u[f] = p.cons_in.f[f][o];
+                if (COMP == kCompHiLo) {
+                    ulo[f] = p.lo_in.f[f][o];
+                }
+            }
+        }
+        if (TMA) {
+            c.timed_out |= !wait_slot<T, NSLOT>(c, nxt);
+        } else {
+            load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, nxt, p, i0, j0, k + 1);
+            __syncthreads();
+        }
+
+        // ---- face phase
+        T const* qc = slot_field<T, TX, TY, NSLOT>(smem, cur, 0);
+        T const* qn = slot_field<T, TX, TY, NSLOT>(smem, nxt, 0);
+        for (int f = tid; f < L::NFACE; f += L::NT) {
+            if (f < L::NFX) {
+                int const fj = f / (TX + 1);
+                int const fi = f % (TX + 1);
+                int const a = (fj + 1) * L::HX + fi;
+                store_flux(fx, L::NFX, f, 0,
+                           hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 0), load_side<T, L::PLANE_PAD>(qc, a + 1, 0)));
+            } else if (f < L::NFX + L::NFY) {
+                int const g = f - L::NFX;
+                int const fj = g / TX;
+                int const fi = g % TX;
+                int const a = fj * L::HX + fi + 1;
+                store_flux(fy, L::NFY, g, 1,
+                           hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 1), load_side<T, L::PLANE_PAD>(qc, a + L::HX, 1)));
+            } else {
+                int const g = f - L::NFX - L::NFY;
+                int const fj = g / TX;
+                int const fi = g % TX;
+                int const a = (fj + 1) * L::HX + fi + 1;
+                store_flux(fz, L::NFZ, g, 2,
+                           hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 2), load_side<T, L::PLANE_PAD>(qn, a, 2)));
+            }
+        }
+        if (__syncthreads_or(c.timed_out)) {
+            return false;
+        }
+        if (TMA) {
+            // plane k is no longer read: refill its slot with plane k+3
+            if (k + 3 <= ke) {
+                if (tid == 0) {
+                    issue_plane<T, TX, TY, NSLOT>(smem, c.bars, cur, maps, i0, j0, k + 3);
+                }
+                c.inflight |= 1u << cur;
+            }
+        }
+
+        // ---- cell phase
+        T fza[5];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            fza[f] = fz[f * L::NFZ + tid];
+        }
+        if (own) {
+            int const xl = tj * (TX + 1) + ti;
+            int const yb = tj * TX + ti;
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                if (COMP == kCompNone) {
+                    T const ax = fx[f * L::NFX + xl + 1] - fx[f * L::NFX + xl];
+                    T const ay = fy[f * L::NFY + yb + TX] - fy[f * L::NFY + yb];
+                    T const az = fza[f] - zlo[f];
+                    u[f] = u[f] - k0 * ax - k1 * ay - k2 * az;
+                } else {
+                    // cons + six signed face terms, summed without
+                    // intermediate rounding error (TwoProduct + TwoSum),
+                    // then rounded once
+                    T sum = u[f];
+                    T err = ulo[f];
+                    compensated_add(sum, err, -k0, fx[f * L::NFX + xl + 1]);
+                    compensated_add(sum, err, k0, fx[f * L::NFX + xl]);
+                    compensated_add(sum, err, -k1, fy[f * L::NFY + yb + TX]);
+                    compensated_add(sum, err, k1, fy[f * L::NFY + yb]);
+                    compensated_add(sum, err, -k2, fza[f]);
+                    compensated_add(sum, err, k2, zlo[f]);
+                    u[f] = sum + err;
+                    ulo[f] = err - (u[f] - sum);
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                p.cons_out.f[f][o] = u[f];
+                if (COMP == kCompHiLo) {
+                    p.lo_out.f[f][o] = ulo[f];
+                }
+            }
+            if (MODE == kModeStep || MODE == kModeStepCons) {
+                // cons_to_prim of the new state (cons_to_prim.hpp:26-31)
+                T const r = rcp_rn(u[0]);
+                T const v0 = u[2] * r;
+                T const v1 = u[3] * r;
+                T const v2 = u[4] * r;
+                T pr;
+                if (MODE == kModeStep) {
+                    T const mm = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
+                    pr = p.gm1 * u[1] - (p.half_gm1 * r) * mm; // (gamma-1)(e - |m|^2/(2 rho))
+                } else {
+                    pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1, COMP == kCompHiLo ? ulo : nullptr);
+                }
+                T const cs = fast_sound_speed((p.gamma * r) * pr);
+                if (MODE == kModeStep) {
+                    p.prim_out.f[0][o] = u[0];
+                    p.prim_out.f[1][o] = pr;
+                    p.prim_out.f[2][o] = v0;
+                    p.prim_out.f[3][o] = v1;
+                    p.prim_out.f[4][o] = v2;
+                    p.cs_out[o] = cs;
+                }
+                // next step's CFL wavespeed (time_step.hpp:28-33)
+                T const invdt = (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
+                long long const key = wave_key(invdt);
+                c.wkey = key > c.wkey ? key : c.wkey;
+                c.bad |= !cell_ok(u[0], pr, invdt);
+            }
+        }
+        // the z face above becomes the next plane's z face below
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            zlo[f] = fza[f];
+        }
+        __syncthreads(); // fluxes are rewritten by the next face phase
+    }
+    return !__syncthreads_or(c.timed_out);
+}
+
+// Block-wide max of the threads' wavespeed keys into *wmax, and the
+// non-physical flag into *status; clears the per-thread values.
+template <class T, int NT>
+__device__ __forceinline__ void flush_wavespeed(TileCtx<T>& c, unsigned long long* wmax, int* status)
+{
+    __shared__ long long warp_best[NT / 32];
+    __shared__ int any_bad;
+    int const tid = threadIdx.x;
+    long long w = c.wkey;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long const v = __shfl_xor_sync(0xffffffffu, w, o);
+        w = v > w ? v : w;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        any_bad = 0;
+    }
+    __syncthreads();
+    if ((tid & 31) == 0) {
+        warp_best[tid >> 5] = w;
+    }
+    if (c.bad) {
+        any_bad = 1;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        long long b = warp_best[0];
+#pragma unroll
+        for (int wv = 1; wv < NT / 32; ++wv) {
+            b = warp_best[wv] > b ? warp_best[wv] : b;
+        }
+        atomicMax(wmax, static_cast<unsigned long long>(b));
+        if (any_bad) {
+            atomicOr(status, 1);
+        }
+    }
+    c.wkey = 0;
+    c.bad = false;
+}
+
+template <class T, int TX, int TY, int NSLOT>
+__device__ __forceinline__ TileCtx<T> make_ctx(unsigned char* smem_dyn)
+{
+    using L = TileLayout<T, TX, TY, NSLOT>;
+    // TMA destinations must sit on 128-byte boundaries of the shared window
+    unsigned char* raw = smem_dyn + ((128u - (smem_u32(smem_dyn) & 127u)) & 127u);
+    TileCtx<T> c;
+    c.bars = reinterpret_cast<unsigned long long*>(raw);
+    c.smem = reinterpret_cast<T*>(raw + L::MBAR_BYTES);
+    c.fx = c.smem + L::FX_OFF;
+    c.fy = c.smem + L::FY_OFF;
+    c.fz = c.smem + L::FZ_OFF;
+    c.phase = 0;
+    c.inflight = 0;
+    c.timed_out = false;
+    c.wkey = 0;
+    c.bad = false;
+    return c;
+}
+
+// dt/dv, from the device dt when there is one (godunov.hpp:37 with the
+// cfl * dt of euler_simulation.cpp:65), evaluated in double.
+template <class T>
+__device__ __forceinline__ T dt_over_dv(FluxParams<T> const& p)
+{
+    if (p.dt_dev != nullptr) {
+        return static_cast<T>((p.cfl * *p.dt_dev) / p.dv);
+    }
+    return p.dtodv;
+}
+
 template <class T, int TX, int TY, int NSLOT, int MODE, bool TMA, int COMP>
 __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant__ FluxParams<T> p,
                                                            const __grid_constant__ TmaMaps maps)
 {
     static_assert(COMP == kCompNone || (sizeof(T) == 4 && MODE == kModeStepCons), "compensation is for the FP32 step");
-    using L = TileLayout<T, TX, TY, NSLOT>;
     static_assert(!TMA || NSLOT == 3, "the TMA ring has three slots");
     extern __shared__ __align__(128) unsigned char smem_dyn[];
-    // TMA destinations must sit on 128-byte boundaries of the shared window
-    unsigned char* smem_raw = smem_dyn + ((128u - (smem_u32(smem_dyn) & 127u)) & 127u);
-    auto* bars = reinterpret_cast<unsigned long long*>(smem_raw);
-    T* smem = reinterpret_cast<T*>(smem_raw + L::MBAR_BYTES);
-    T* fx = smem + L::FX_OFF;
-    T* fy = smem + L::FY_OFF;
-    T* fz = smem + L::FZ_OFF;
-
-    T dtodv = p.dtodv;
-    if (p.dt_dev != nullptr) {
-        double const dtc = p.cfl * *p.dt_dev;    // cfl * dt, euler_simulation.cpp:65
-        dtodv = static_cast<T>(dtc / p.dv);      // godunov.hpp:37
-    }
+    TileCtx<T> c = make_ctx<T, TX, TY, NSLOT>(smem_dyn);
+    T const dtodv = dt_over_dv(p);
     // cons -= dt/dv * sum_d ds_d (F_R - F_L), coefficients folded
     T const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2;
 
-    int const tid = threadIdx.x;
-    int const ti = tid % TX;
-    int const tj = tid / TX;
-    int const center = (tj + 1) * L::HX + ti + 1;
-
-    long long wkey = 0;
-    bool bad = false;
-    unsigned phase = 0;    // bit s: parity of slot s's next completion (TMA ring)
-    unsigned inflight = 0; // bit s: a TMA into slot s has not been waited for
-    bool timed_out = false;
-
     if (TMA) {
-        if (tid == 0) {
+        if (threadIdx.x == 0) {
             for (int s = 0; s < NSLOT; ++s) {
-                mbar_init(&bars[s], 1);
+                mbar_init(&c.bars[s], 1);
             }
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
         __syncthreads();
     }
 
-    auto wait_slot = [&](int s) -> bool {
-        bool const ok = mbar_wait(&bars[s], (phase >> s) & 1u);
-        phase ^= 1u << s;
-        inflight &= ~(1u << s);
-        return ok;
-    };
-
     int const tiles_xy = p.tiles_x * p.tiles_y;
     for (int w = blockIdx.x; w < p.nwork; w += gridDim.x) {
         int const tx = w % p.tiles_x;
         int const ty = (w / p.tiles_x) % p.tiles_y;
         int const kc = w / tiles_xy;
-        int const i0 = 1 + tx * TX;
-        int const j0 = 1 + ty * TY;
-        int const kb = 1 + kc * p.kchunk;
-        int const ke = min(kb + p.kchunk, p.g.n2 - 1);
-        int const i = i0 + ti;
-        int const j = j0 + tj;
-        bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
-
-        __syncthreads(); // the previous item's readers of slots and fluxes are done
-        if (TMA) {
-            // planes kb-1, kb, kb+1 -> slots 0, 1, 2 (kb+1 <= ke always)
-            if (tid == 0) {
-                issue_plane<T, TX, TY, NSLOT>(smem, bars, 0, maps, i0, j0, kb - 1);
-                issue_plane<T, TX, TY, NSLOT>(smem, bars, 1, maps, i0, j0, kb);
-                issue_plane<T, TX, TY, NSLOT>(smem, bars, 2, maps, i0, j0, kb + 1);
-            }
-            inflight |= 7u;
-            timed_out |= !wait_slot(0);
-            timed_out |= !wait_slot(1);
-        } else {
-            load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, 0, p, i0, j0, kb - 1);
-            load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, 1, p, i0, j0, kb);
-            __syncthreads();
-        }
-        // z face below the chunk's first plane, kept in registers in global
-        // axes (the z face frame has n = mx2, t1 = mx0, t2 = mx1)
-        T zlo[5];
-        {
-            Flux<T> const f0 =
-                    hllc_flux(load_side<T, L::PLANE_PAD>(slot_field<T, TX, TY, NSLOT>(smem, 0, 0), center, 2),
-                              load_side<T, L::PLANE_PAD>(slot_field<T, TX, TY, NSLOT>(smem, 1, 0), center, 2));
-            zlo[0] = f0.d;
-            zlo[1] = f0.e;
-            zlo[2] = f0.t1;
-            zlo[3] = f0.t2;
-            zlo[4] = f0.n;
-        }
-        if (__syncthreads_or(timed_out)) { // slot 0 is refilled next
-            break;
-        }
-        if (TMA) {
-            if (kb + 2 <= ke) {
-                if (tid == 0) {
-                    issue_plane<T, TX, TY, NSLOT>(smem, bars, 0, maps, i0, j0, kb + 2);
-                }
-                inflight |= 1u;
-            }
-        }
-
-        for (int k = kb; k < ke; ++k) {
-            int const cur = (k - kb + 1) % NSLOT;
-            int const nxt = (k - kb + 2) % NSLOT;
-            // this cell's conservative state, fetched while the faces are solved
-            T u[5];
-            T ulo[5] = {T(0), T(0), T(0), T(0), T(0)};
-            long long const o = p.g.at(i, j, k);
-            if (own) {
-#pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    u[f] = p.cons_in.f[f][o];
-                    if (COMP == kCompHiLo) {
-                        ulo[f] = p.lo_in.f[f][o];
-                    }
-                }
-            }
-            if (TMA) {
-                timed_out |= !wait_slot(nxt);
-            } else {
-                load_plane<T, TX, TY, NSLOT, MODE, COMP>(smem, nxt, p, i0, j0, k + 1);
-                __syncthreads();
-            }
-
-            // ---- face phase
-            T const* qc = slot_field<T, TX, TY, NSLOT>(smem, cur, 0);
-            T const* qn = slot_field<T, TX, TY, NSLOT>(smem, nxt, 0);
-            for (int f = tid; f < L::NFACE; f += L::NT) {
-                if (f < L::NFX) {
-                    int const fj = f / (TX + 1);
-                    int const fi = f % (TX + 1);
-                    int const a = (fj + 1) * L::HX + fi;
-                    store_flux(fx, L::NFX, f, 0,
-                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 0), load_side<T, L::PLANE_PAD>(qc, a + 1, 0)));
-                } else if (f < L::NFX + L::NFY) {
-                    int const g = f - L::NFX;
-                    int const fj = g / TX;
-                    int const fi = g % TX;
-                    int const a = fj * L::HX + fi + 1;
-                    store_flux(fy, L::NFY, g, 1,
-                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 1),
-                                         load_side<T, L::PLANE_PAD>(qc, a + L::HX, 1)));
-                } else {
-                    int const g = f - L::NFX - L::NFY;
-                    int const fj = g / TX;
-                    int const fi = g % TX;
-                    int const a = (fj + 1) * L::HX + fi + 1;
-                    store_flux(fz, L::NFZ, g, 2,
-                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 2), load_side<T, L::PLANE_PAD>(qn, a, 2)));
-                }
-            }
-            if (__syncthreads_or(timed_out)) {
-                break;
-            }
-            if (TMA) {
-                // plane k is no longer read: refill its slot with plane k+3
-                if (k + 3 <= ke) {
-                    if (tid == 0) {
-                        issue_plane<T, TX, TY, NSLOT>(smem, bars, cur, maps, i0, j0, k + 3);
-                    }
-                    inflight |= 1u << cur;
-                }
-            }
-
-            // ---- cell phase
-            T fza[5];
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                fza[f] = fz[f * L::NFZ + tid];
-            }
-            if (own) {
-                int const xl = tj * (TX + 1) + ti;
-                int const yb = tj * TX + ti;
-#pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    if (COMP == kCompNone) {
-                        T const ax = fx[f * L::NFX + xl + 1] - fx[f * L::NFX + xl];
-                        T const ay = fy[f * L::NFY + yb + TX] - fy[f * L::NFY + yb];
-                        T const az = fza[f] - zlo[f];
-                        u[f] = u[f] - k0 * ax - k1 * ay - k2 * az;
-                    } else {
-                        // cons + six signed face terms, summed without
-                        // intermediate rounding error (TwoProduct +
-                        // TwoSum), then rounded once
-                        T sum = u[f];
-                        T err = ulo[f];
-                        compensated_add(sum, err, -k0, fx[f * L::NFX + xl + 1]);
-                        compensated_add(sum, err, k0, fx[f * L::NFX + xl]);
-                        compensated_add(sum, err, -k1, fy[f * L::NFY + yb + TX]);
-                        compensated_add(sum, err, k1, fy[f * L::NFY + yb]);
-                        compensated_add(sum, err, -k2, fza[f]);
-                        compensated_add(sum, err, k2, zlo[f]);
-                        u[f] = sum + err;
-                        ulo[f] = err - (u[f] - sum);
-                    }
-                }
-#pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    p.cons_out.f[f][o] = u[f];
-                    if (COMP == kCompHiLo) {
-                        p.lo_out.f[f][o] = ulo[f];
-                    }
-                }
-                if (MODE == kModeStep || MODE == kModeStepCons) {
-                    // cons_to_prim of the new state (cons_to_prim.hpp:26-31)
-                    T const r = rcp_rn(u[0]);
-                    T const v0 = u[2] * r;
-                    T const v1 = u[3] * r;
-                    T const v2 = u[4] * r;
-                    T pr;
-                    if (MODE == kModeStep) {
-                        T const mm = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
-                        pr = p.gm1 * u[1] - (p.half_gm1 * r) * mm; // (gamma-1)(e - |m|^2/(2 rho))
-                    } else {
-                        pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1,
-                                                 COMP == kCompHiLo ? ulo : nullptr);
-                    }
-                    T const cs = fast_sound_speed((p.gamma * r) * pr);
-                    if (MODE == kModeStep) {
-                        p.prim_out.f[0][o] = u[0];
-                        p.prim_out.f[1][o] = pr;
-                        p.prim_out.f[2][o] = v0;
-                        p.prim_out.f[3][o] = v1;
-                        p.prim_out.f[4][o] = v2;
-                        p.cs_out[o] = cs;
-                    }
-                    // next step's CFL wavespeed (time_step.hpp:28-33)
-                    T const invdt =
-                            (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
-                    long long const key = wave_key(invdt);
-                    wkey = key > wkey ? key : wkey;
-                    bad |= !cell_ok(u[0], pr, invdt);
-                }
-            }
-            // the z face above becomes the next plane's z face below
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                zlo[f] = fza[f];
-            }
-            __syncthreads(); // fluxes are rewritten by the next face phase
-        }
-        if (__syncthreads_or(timed_out)) {
+        if (!tile_item<T, TX, TY, NSLOT, MODE, TMA, COMP>(c, p, maps, k0, k1, k2, tx, ty, kc)) {
             break;
         }
     }
 
-    if (TMA && __syncthreads_or(timed_out)) {
+    if (TMA && __syncthreads_or(c.timed_out)) {
         // a staged plane never arrived: report, wait (bounded) for the copies
         // still in flight so none lands after the CTA is gone, and stop
-        if (tid == 0) {
+        if (threadIdx.x == 0) {
             atomicOr(p.status, 2);
         }
         for (int s = 0; s < NSLOT; ++s) {
-            if (inflight & (1u << s)) {
-                wait_slot(s);
+            if (c.inflight & (1u << s)) {
+                wait_slot<T, NSLOT>(c, s);
             }
         }
         return;
     }
-
     if (MODE == kModeStep || MODE == kModeStepCons) {
-        __shared__ long long warp_best[TX * TY / 32];
-        __shared__ int any_bad;
+        flush_wavespeed<T, TX * TY>(c, p.wmax, p.status);
+    }
+}
+
+// Many independent grids in one launch: a persistent grid of CTAs pops
+// (grid, tile, chunk) items from a global queue (largest grids first),
+// copies the item's grid parameters to shared memory and runs the same tile
+// engine; each item's wavespeed goes to its own grid's accumulator, so every
+// grid keeps its own dt.  Plain-load staging (grids of any shape).
+template <class T, int TX, int TY, int MODE, int COMP>
+__global__ void __launch_bounds__(TX* TY) flux_batch_kernel(const __grid_constant__ BatchParams<T> b)
+{
+    constexpr int NSLOT = 2;
+    constexpr int NT = TX * TY;
+    static_assert(sizeof(FluxParams<T>) % 4 == 0 && sizeof(FluxParams<T>) / 4 <= NT, "parameter copy");
+    extern __shared__ __align__(128) unsigned char smem_dyn[];
+    __shared__ __align__(16) FluxParams<T> gp;
+    __shared__ int s_item;
+    TileCtx<T> c = make_ctx<T, TX, TY, NSLOT>(smem_dyn);
+    int const tid = threadIdx.x;
+    for (;;) {
+        __syncthreads(); // everyone is done with the previous item's parameters
         if (tid == 0) {
-            any_bad = 0;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            long long const v = __shfl_xor_sync(0xffffffffu, wkey, o);
-            wkey = v > wkey ? v : wkey;
+            s_item = static_cast<int>(atomicAdd(b.head, 1u));
         }
         __syncthreads();
-        if ((tid & 31) == 0) {
-            warp_best[tid >> 5] = wkey;
+        int const item = s_item;
+        if (item >= b.nitems) {
+            break;
         }
-        if (bad) {
-            any_bad = 1;
+        int4 const it = b.items[item];
+        if (tid < static_cast<int>(sizeof(FluxParams<T>) / 4)) {
+            reinterpret_cast<int*>(&gp)[tid] = reinterpret_cast<const int*>(&b.grids[it.x])[tid];
         }
         __syncthreads();
-        if (tid == 0) {
-            long long b = warp_best[0];
-#pragma unroll
-            for (int wv = 1; wv < TX * TY / 32; ++wv) {
-                b = warp_best[wv] > b ? warp_best[wv] : b;
-            }
-            atomicMax(p.wmax, static_cast<unsigned long long>(b));
-            if (any_bad) {
-                atomicOr(p.status, 1);
-            }
-        }
+        T const dtodv = dt_over_dv(gp);
+        T const k0 = dtodv * gp.ds0, k1 = dtodv * gp.ds1, k2 = dtodv * gp.ds2;
+        tile_item<T, TX, TY, NSLOT, MODE, false, COMP>(c, gp, TmaMaps{}, k0, k1, k2, it.y, it.z, it.w);
+        flush_wavespeed<T, NT>(c, gp.wmax, gp.status);
     }
 }
 
@@ -565,7 +656,7 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant
 // (bit-identical to the reference's cons_to_prim over ghosts,
 // cons_to_prim.hpp:26-27), sound speed and CFL contribution.
 template <class T>
-__global__ void __launch_bounds__(256) ghost_shell_kernel(GhostParams<T> p)
+__device__ __forceinline__ void ghost_shell_body(GhostParams<T> const& p)
 {
     Geom const g = p.g;
     bool const all = (g.n0 < 3) || (g.n1 < 3) || (g.n2 < 3);
@@ -652,21 +743,55 @@ __global__ void __launch_bounds__(256) ghost_shell_kernel(GhostParams<T> p)
     }
 }
 
+template <class T>
+__global__ void __launch_bounds__(256) ghost_shell_kernel(GhostParams<T> p)
+{
+    ghost_shell_body(p);
+}
+
+// Ghost shells of every grid of a batch: blockIdx.y selects the grid.
+template <class T>
+__global__ void __launch_bounds__(256) ghost_batch_kernel(const GhostParams<T>* gps)
+{
+    GhostParams<T> const p = gps[blockIdx.y];
+    ghost_shell_body(p);
+}
+
 // Turns the max-wavespeed accumulator into the next step's dt
 // (time_step.hpp:34-39: min over cells of 1/invdt == 1/max invdt), adds the
 // step just taken to the simulated time and clears the accumulator.
 template <class T>
+__device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time)
+{
+    if (add_time) {
+        s->t += static_cast<double>(cfl * static_cast<T>(s->dt));
+        s->steps += 1;
+    }
+    T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(s->wmax)));
+    T const dt = (m > T(0)) ? rcp_rn(m) : (sizeof(T) == 8 ? T(DBL_MAX) : T(FLT_MAX));
+    s->dt = static_cast<double>(dt);
+    s->wmax = 0ull;
+}
+
+template <class T>
 __global__ void finalize_dt_kernel(SimScalars* s, T cfl, int add_time)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        if (add_time) {
-            s->t += static_cast<double>(cfl * static_cast<T>(s->dt));
-            s->steps += 1;
-        }
-        T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(s->wmax)));
-        T const dt = (m > T(0)) ? rcp_rn(m) : (sizeof(T) == 8 ? T(DBL_MAX) : T(FLT_MAX));
-        s->dt = static_cast<double>(dt);
-        s->wmax = 0ull;
+        finalize_one(s, cfl, add_time);
+    }
+}
+
+// Every grid of a batch, and the work-queue head back to zero for the next
+// launch of the batch kernel.
+template <class T>
+__global__ void finalize_batch_kernel(SimScalars* s, int ngrids, T cfl, int add_time, unsigned* head)
+{
+    int const g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < ngrids) {
+        finalize_one(&s[g], cfl, add_time);
+    }
+    if (g == 0 && head != nullptr) {
+        *head = 0u;
     }
 }
 
@@ -755,7 +880,90 @@ cudaError_t launch_flux_impl(FluxParams<T> p, TmaMaps const& maps, int sms, cuda
     return cudaGetLastError();
 }
 
+// Tile shapes the batch kernel is built for (the autotuner picks one).
+constexpr int kBatchShapes[][2] = {{32, 8}, {16, 8}, {16, 16}};
+constexpr int kNumBatchShapes = 3;
+
+template <class T, int TX, int TY, int MODE, int COMP>
+struct BatchKernel {
+    using L = TileLayout<T, TX, TY, 2>;
+    static auto fn() { return flux_batch_kernel<T, TX, TY, MODE, COMP>; }
+    static cudaError_t configure(int* per_sm)
+    {
+        auto kern = fn();
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(L::BYTES));
+        if (e != cudaSuccess) {
+            return e;
+        }
+        int n = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, L::NT, L::BYTES);
+        *per_sm = n < 1 ? 1 : n;
+        return e;
+    }
+    static cudaError_t launch(BatchParams<T> const& b, int grid, cudaStream_t s)
+    {
+        fn()<<<grid, L::NT, L::BYTES, s>>>(b);
+        return cudaGetLastError();
+    }
+};
+
+template <class T, int MODE, int COMP>
+cudaError_t batch_dispatch(int shape, BatchParams<T> const* b, int grid, int* per_sm, cudaStream_t s)
+{
+    switch (shape) {
+    case 0: return b ? BatchKernel<T, 32, 8, MODE, COMP>::launch(*b, grid, s) : BatchKernel<T, 32, 8, MODE, COMP>::configure(per_sm);
+    case 1: return b ? BatchKernel<T, 16, 8, MODE, COMP>::launch(*b, grid, s) : BatchKernel<T, 16, 8, MODE, COMP>::configure(per_sm);
+    default: return b ? BatchKernel<T, 16, 16, MODE, COMP>::launch(*b, grid, s) : BatchKernel<T, 16, 16, MODE, COMP>::configure(per_sm);
+    }
+}
+
 } // namespace
+
+int batch_shape_count() { return kNumBatchShapes; }
+void batch_shape(int shape, int* tx, int* ty)
+{
+    *tx = kBatchShapes[shape][0];
+    *ty = kBatchShapes[shape][1];
+}
+
+// b == nullptr: configure (dynamic shared memory opt-in) and report the
+// resident CTAs per SM; otherwise launch `grid` persistent CTAs.
+template <class T>
+cudaError_t launch_flux_batch(int shape, int comp, BatchParams<T> const* b, int grid, int* per_sm, cudaStream_t s)
+{
+    if constexpr (sizeof(T) == sizeof(double)) {
+        return batch_dispatch<double, kModeStep, kCompNone>(shape, b, grid, per_sm, s);
+    } else {
+        switch (comp) {
+        case kCompSum: return batch_dispatch<float, kModeStepCons, kCompSum>(shape, b, grid, per_sm, s);
+        case kCompHiLo: return batch_dispatch<float, kModeStepCons, kCompHiLo>(shape, b, grid, per_sm, s);
+        default: return batch_dispatch<float, kModeStepCons, kCompNone>(shape, b, grid, per_sm, s);
+        }
+    }
+}
+
+template <class T>
+cudaError_t launch_ghost_batch(GhostParams<T> const* gps, int ngrids, int blocks_per_grid, cudaStream_t s)
+{
+    dim3 grid(static_cast<unsigned>(blocks_per_grid), static_cast<unsigned>(ngrids));
+    ghost_batch_kernel<T><<<grid, 256, 0, s>>>(gps);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_finalize_batch(SimScalars* sc, int ngrids, T cfl, int add_time, unsigned* head, cudaStream_t s)
+{
+    finalize_batch_kernel<T><<<(ngrids + 255) / 256, 256, 0, s>>>(sc, ngrids, cfl, add_time, head);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_flux_batch<double>(int, int, BatchParams<double> const*, int, int*, cudaStream_t);
+template cudaError_t launch_flux_batch<float>(int, int, BatchParams<float> const*, int, int*, cudaStream_t);
+template cudaError_t launch_ghost_batch<double>(GhostParams<double> const*, int, int, cudaStream_t);
+template cudaError_t launch_ghost_batch<float>(GhostParams<float> const*, int, int, cudaStream_t);
+template cudaError_t launch_finalize_batch<double>(SimScalars*, int, double, int, unsigned*, cudaStream_t);
+template cudaError_t launch_finalize_batch<float>(SimScalars*, int, float, int, unsigned*, cudaStream_t);
 
 template <class T>
 struct FluxDispatch;

@@ -57,6 +57,15 @@ struct FluxParams {
     int per_sm;                          // resident CTAs per SM (from configure_flux)
 };
 
+// Launch parameters of the multi-grid batch kernel.
+template <class T>
+struct BatchParams {
+    const FluxParams<T>* grids; // per grid, for this step's copy direction
+    const int4* items;          // work items (grid, tile x, tile y, chunk), largest grids first
+    int nitems;
+    unsigned* head;             // work-queue head; zero before each launch
+};
+
 template <class T>
 struct GhostParams {
     Geom g;
@@ -86,6 +95,8 @@ cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1
                              int sms, cudaStream_t s);
 template <class T>
 cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s);
+cudaError_t launch_init_step(Bundle<double> prim, Geom g, double dx0, double dx1, double dx2, double c,
+                             double rho_in, double p_in, double rho_out, double p_out, int sms, cudaStream_t s);
 // max invdt over all cells of a cons-only FP32 state (compensated: FP64
 // internal energy for low-pressure cells)
 cudaError_t launch_invdt_max_cons(CBundle<float> cons, long long n, float gamma, float ix0, float ix1, float ix2,
@@ -98,6 +109,16 @@ template <class T>
 cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int comp, int sms, cudaStream_t s);
 int flux_tile_x();
 int flux_tile_y();
+
+// Multi-grid batch (batch.cu): tile-shape variants of the batch kernel.
+int batch_shape_count();
+void batch_shape(int shape, int* tx, int* ty);
+template <class T>
+cudaError_t launch_flux_batch(int shape, int comp, BatchParams<T> const* b, int grid, int* per_sm, cudaStream_t s);
+template <class T>
+cudaError_t launch_ghost_batch(GhostParams<T> const* gps, int ngrids, int blocks_per_grid, cudaStream_t s);
+template <class T>
+cudaError_t launch_finalize_batch(SimScalars* sc, int ngrids, T cfl, int add_time, unsigned* head, cudaStream_t s);
 template <class T>
 cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s);
 template <class T>

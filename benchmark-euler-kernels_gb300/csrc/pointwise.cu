@@ -218,6 +218,35 @@ __global__ void __launch_bounds__(256) sound_speed_kernel(CBundle<T> prim, T* cs
     }
 }
 
+// ----------------------------------------------------------- init_step
+// Step discontinuity on x + y + z < c, the initial condition of the batched
+// workload (it has no counterpart in the reference): cell centres
+// ((i-1)+0.5) dx in double as in init_implode.hpp:33-36 but on [0,1]^3,
+// (rho_in, p_in) below the plane, (rho_out, p_out) above it, u = 0.
+template <class T>
+__global__ void __launch_bounds__(256) init_step_kernel(Bundle<T> prim, Geom g, double dx0, double dx1, double dx2,
+                                                        double c, double rho_in, double p_in, double rho_out,
+                                                        double p_out)
+{
+    long long const n = g.ncell();
+    for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < n;
+         idx += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int const i = static_cast<int>(idx % g.n0);
+        long long const jk = idx / g.n0;
+        int const j = static_cast<int>(jk % g.n1);
+        int const k = static_cast<int>(jk / g.n1);
+        double const x0 = __dmul_rn(__dadd_rn(static_cast<double>(i - 1), 0.5), dx0);
+        double const x1 = __dmul_rn(__dadd_rn(static_cast<double>(j - 1), 0.5), dx1);
+        double const x2 = __dmul_rn(__dadd_rn(static_cast<double>(k - 1), 0.5), dx2);
+        bool const inside = __dadd_rn(__dadd_rn(x0, x1), x2) < c;
+        prim.f[0][idx] = static_cast<T>(inside ? rho_in : rho_out);
+        prim.f[1][idx] = static_cast<T>(inside ? p_in : p_out);
+        prim.f[2][idx] = T(0);
+        prim.f[3][idx] = T(0);
+        prim.f[4][idx] = T(0);
+    }
+}
+
 // ------------------------------------------------------------------ launch
 static int grid_for(long long n, int sms)
 {
@@ -271,6 +300,14 @@ template <class T>
 cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s)
 {
     sound_speed_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cs, n, gamma);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_step(Bundle<double> prim, Geom g, double dx0, double dx1, double dx2, double c,
+                             double rho_in, double p_in, double rho_out, double p_out, int sms, cudaStream_t s)
+{
+    init_step_kernel<double><<<grid_for(g.ncell(), sms), 256, 0, s>>>(prim, g, dx0, dx1, dx2, c, rho_in, p_in, rho_out,
+                                                                       p_out);
     return cudaGetLastError();
 }
 

@@ -33,6 +33,12 @@ class EulerError(RuntimeError):
         self.status = status
 
 
+class GridDesc(ctypes.Structure):
+    """eulr_grid_desc: extents (ghosts included), gamma, spacings."""
+    _fields_ = [("n0", ctypes.c_int), ("n1", ctypes.c_int), ("n2", ctypes.c_int), ("gamma", ctypes.c_double),
+                ("dx0", ctypes.c_double), ("dx1", ctypes.c_double), ("dx2", ctypes.c_double)]
+
+
 class Bundle5(ctypes.Structure):
     """Five field pointers (eulr_prim_* / eulr_cons_*; const or not)."""
     _fields_ = [("f0", ctypes.c_void_p), ("f1", ctypes.c_void_p), ("f2", ctypes.c_void_p),
@@ -73,6 +79,17 @@ _SIGNATURES = [
     ("eulr_sim_totals", _I, [_P, ctypes.POINTER(_D)]),
     ("eulr_sim_state_bytes", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("eulr_probe_fma_rate", _I, [_I, _I, ctypes.POINTER(_D)]),
+    ("eulr_batch_create", _I, [_I, _I, _P, _D, _P, ctypes.POINTER(_P)]),
+    ("eulr_batch_destroy", _I, [_P]),
+    ("eulr_batch_set_prim_f64", _I, [_P, _I, Bundle5]),
+    ("eulr_batch_init_step", _I, [_P, _I, _D, _D, _D, _D, _D]),
+    ("eulr_batch_autotune", _I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D)]),
+    ("eulr_batch_advance", _I, [_P, _I]),
+    ("eulr_batch_get_state_f64", _I, [_P, _I, Bundle5, Bundle5]),
+    ("eulr_batch_time", _I, [_P, _I, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_longlong)]),
+    ("eulr_batch_status", _I, [_P]),
+    ("eulr_batch_info", _I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                             ctypes.POINTER(_I)]),
 ]
 
 # Every symbol include/euler_gb300.h declares (checked by the CPU tests).
@@ -293,6 +310,77 @@ class Simulation:
         out = ctypes.c_longlong()
         check(load().eulr_sim_state_bytes(self._h, ctypes.byref(out)))
         return out.value
+
+
+class Batch:
+    """Multi-grid batch (eulr_batch_*): uneven grids, one persistent launch per step."""
+
+    def __init__(self, grids, cfl=0.4, precision="f64", stream=None):
+        """grids: sequence of (n0, n1, n2, gamma, dx0, dx1, dx2), extents with ghosts."""
+        self.shapes = [tuple(int(v) for v in g[:3]) for g in grids]
+        arr = (GridDesc * len(grids))(*[GridDesc(*[int(v) for v in g[:3]], *[float(v) for v in g[3:7]])
+                                        for g in grids])
+        h = ctypes.c_void_p()
+        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else ctypes.c_void_p(None)
+        check(load().eulr_batch_create(PRECISION[precision], len(grids), ctypes.cast(arr, ctypes.c_void_p),
+                                       float(cfl), s, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().eulr_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_prim(self, g, prim):
+        check(load().eulr_batch_set_prim_f64(self._h, int(g), bundle(prim)))
+
+    def init_step(self, g, c, rho_in, p_in, rho_out=1.0, p_out=1.0):
+        check(load().eulr_batch_init_step(self._h, int(g), float(c), float(rho_in), float(p_in), float(rho_out),
+                                          float(p_out)))
+
+    def autotune(self, trial_steps=2):
+        shape, kc, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        check(load().eulr_batch_autotune(self._h, int(trial_steps), ctypes.byref(shape), ctypes.byref(kc),
+                                         ctypes.byref(ms)))
+        return {"tile": (shape.value // 1000, shape.value % 1000), "kchunk": kc.value, "step_ms": ms.value}
+
+    def advance(self, nsteps):
+        check(load().eulr_batch_advance(self._h, int(nsteps)))
+
+    def state_numpy(self, g):
+        import numpy as np
+        n0, n1, n2 = self.shapes[g]
+        prim = np.zeros((5, n2, n1, n0))
+        cons = np.zeros((5, n2, n1, n0))
+        check(load().eulr_batch_get_state_f64(self._h, int(g), bundle(prim), bundle(cons)))
+        return prim, cons
+
+    def time(self, g):
+        t, dt, st = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        check(load().eulr_batch_time(self._h, int(g), ctypes.byref(t), ctypes.byref(dt), ctypes.byref(st)))
+        return t.value, dt.value, st.value
+
+    def status(self) -> int:
+        return load().eulr_batch_status(self._h)
+
+    def info(self):
+        cells, items, shape, kc = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(load().eulr_batch_info(self._h, ctypes.byref(cells), ctypes.byref(items), ctypes.byref(shape),
+                                     ctypes.byref(kc)))
+        return {"interior_cells": cells.value, "items": items.value,
+                "tile": (shape.value // 1000, shape.value % 1000), "kchunk": kc.value}
 
 
 def fma_rate(kind: str = "f64", iters: int = 20000) -> float:

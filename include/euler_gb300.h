@@ -260,6 +260,51 @@ int eulr_sim_totals(eulr_sim* sim, double out[5]);
  * state's word size). */
 int eulr_sim_state_bytes(eulr_sim* sim, long long* bytes_per_step);
 
+/* -------------------------------------------------------- multi-grid batch
+ * Many independent grids of uneven sizes, each with its own gamma, mesh and
+ * dt, advanced together: one persistent kernel launch per step pulls
+ * (grid, tile, chunk) work items from a device work queue (largest grids
+ * first), and pairs of steps replay from a CUDA graph.  The tile shape and
+ * chunk length are chosen by eulr_batch_autotune.  Loading functions work on
+ * the batch's first state copy: load every grid before the first step (or
+ * after an even number of steps). */
+typedef struct eulr_batch eulr_batch;
+
+typedef struct eulr_grid_desc {
+    int n0, n1, n2;          /* cells per axis, ghosts included */
+    double gamma;            /* ratio of specific heats */
+    double dx0, dx1, dx2;    /* mesh spacings */
+} eulr_grid_desc;
+
+int eulr_batch_create(int precision, int ngrids, const eulr_grid_desc* grids, double cfl, eulr_stream_t stream,
+                      eulr_batch** out);
+int eulr_batch_destroy(eulr_batch* batch);
+
+/* Load grid `grid` from an FP64 prim bundle (host or device); cons is
+ * prim_to_cons of it. */
+int eulr_batch_set_prim_f64(eulr_batch* batch, int grid, eulr_prim_cf64 prim);
+
+/* Step initial condition of the batched workload (no counterpart in the
+ * reference): cell centres x_d = ((i_d - 1) + 0.5) dx_d on [0,1]^3,
+ * (rho_in, p_in) where x0 + x1 + x2 < c, (rho_out, p_out) elsewhere, u = 0. */
+int eulr_batch_init_step(eulr_batch* batch, int grid, double c, double rho_in, double p_in, double rho_out,
+                         double p_out);
+
+/* Times every tile shape (32x8, 16x8, 16x16) and chunk length (8, 16, 32,
+ * 64 planes) on the loaded state over `trial_steps` steps each, keeps the
+ * fastest and restores the state's clocks.  Reports the choice as
+ * TX*1000+TY, the chunk length and its step time in ms (any may be NULL). */
+int eulr_batch_autotune(eulr_batch* batch, int trial_steps, int* tile_shape, int* kchunk, double* step_ms);
+
+int eulr_batch_advance(eulr_batch* batch, int nsteps);
+int eulr_batch_get_state_f64(eulr_batch* batch, int grid, eulr_prim_f64 prim, eulr_cons_f64 cons);
+int eulr_batch_time(eulr_batch* batch, int grid, double* t, double* next_dt, long long* steps);
+/* EULR_ERR_NONFINITE when any grid produced a non-physical cell. */
+int eulr_batch_status(eulr_batch* batch);
+/* Interior cells of all grids, work items per step, tile shape (TX*1000+TY)
+ * and chunk length in use (any may be NULL). */
+int eulr_batch_info(eulr_batch* batch, long long* interior_cells, int* nitems, int* tile_shape, int* kchunk);
+
 /* ------------------------------------------------------------ measurement */
 
 /* Times `iters` launches of a kernel whose warps issue only dependent-free

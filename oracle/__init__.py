@@ -99,6 +99,16 @@ def init_implode(n0, n1, n2, dx, dtype=np.float64, impl="port") -> np.ndarray:
     return prim
 
 
+def init_step(n0, n1, n2, dx, c, rho_in, p_in, rho_out=1.0, p_out=1.0, dtype=np.float64) -> np.ndarray:
+    """Step initial condition of the batched workload (x0 + x1 + x2 < c), port only."""
+    prim = empty_bundle(n0, n1, n2, dtype)
+    suf = _suffix(prim)
+    D = ctypes.c_double
+    _fn("port", "init_step", suf)(_ptrs(prim), n0, n1, n2, D(dx[0]), D(dx[1]), D(dx[2]), D(c), D(rho_in), D(p_in),
+                                  D(rho_out), D(p_out))
+    return prim
+
+
 def prim_to_cons(prim: np.ndarray, gamma: float, impl="port") -> np.ndarray:
     cons = np.zeros_like(prim)
     suf = _suffix(prim)

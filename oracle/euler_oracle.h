@@ -13,6 +13,8 @@ extern "C" {
 
 #define EULER_ORACLE_DECLARE(SUF, REAL)                                                            \
     void oracle_init_implode_##SUF(REAL* const* prim, int n0, int n1, int n2, REAL dx0, REAL dx1, REAL dx2); \
+    void oracle_init_step_##SUF(REAL* const* prim, int n0, int n1, int n2, double dx0, double dx1, double dx2,   \
+                                double c, double rho_in, double p_in, double rho_out, double p_out);      \
     void oracle_prim_to_cons_##SUF(REAL const* const* prim, REAL* const* cons, int n0, int n1, int n2, REAL gamma); \
     void oracle_cons_to_prim_##SUF(REAL const* const* cons, REAL* const* prim, int n0, int n1, int n2, REAL gamma); \
     REAL oracle_time_step_##SUF(REAL const* const* prim, int n0, int n1, int n2, REAL gamma, REAL dx0, REAL dx1, REAL dx2); \

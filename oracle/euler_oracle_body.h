@@ -121,6 +121,31 @@ void FN(oracle_init_implode)(REAL* const* prim, int n0, int n1, int n2, REAL dx0
     }
 }
 
+/* Step initial condition of the batched workload (no reference counterpart):
+ * cell centres ((i-1)+0.5) dx on [0,1]^3 in double, (rho_in, p_in) where
+ * x0 + x1 + x2 < c, (rho_out, p_out) elsewhere, u = 0. */
+void FN(oracle_init_step)(REAL* const* prim, int n0, int n1, int n2, double dx0, double dx1, double dx2, double c,
+                          double rho_in, double p_in, double rho_out, double p_out)
+{
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < n2; ++k) {
+        for (int j = 0; j < n1; ++j) {
+            for (int i = 0; i < n0; ++i) {
+                double const x0 = ((double)(i - 1) + 0.5) * dx0;
+                double const x1 = ((double)(j - 1) + 0.5) * dx1;
+                double const x2 = ((double)(k - 1) + 0.5) * dx2;
+                int const inside = (x0 + x1) + x2 < c;
+                size_t const o = (size_t)i + (size_t)n0 * ((size_t)j + (size_t)n1 * (size_t)k);
+                prim[0][o] = (REAL)(inside ? rho_in : rho_out);
+                prim[1][o] = (REAL)(inside ? p_in : p_out);
+                prim[2][o] = 0;
+                prim[3][o] = 0;
+                prim[4][o] = 0;
+            }
+        }
+    }
+}
+
 /* prim_to_cons, prim_to_cons.hpp:7-33 with to_cons (euler_arrays.hpp:56-64)
  * and PerfectGas::internal_energy (perfect_gas.hpp:20-23). */
 void FN(oracle_prim_to_cons)(REAL const* const* prim, REAL* const* cons, int n0, int n1, int n2, REAL gamma)

@@ -1,0 +1,116 @@
+"""GPU tests of the multi-grid batch (eulr_batch_*): every grid of a batch
+of uneven grids -- each with its own gamma, mesh and dt -- against the oracle
+run on that grid alone; tile-shape independence (the autotuned tiling gives
+bit-identical results); and identity with the single-grid simulation."""
+import numpy as np
+import pytest
+
+from conftest import rel_linf
+
+pytestmark = pytest.mark.gpu
+
+
+def draw_batch(seed, sizes=(24, 32, 48), ngrids=6):
+    """Grids like the batched workload: axis lengths from `sizes`, gamma
+    U[1.1, 1.67], inner/outer pressure ratio log-U[0.01, 1], density ratio
+    log-U[0.05, 1], step on x+y+z < c with c U[0.1, 0.5]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    grids, ics = [], []
+    for _ in range(ngrids):
+        n = [int(rng.choice(sizes)) for _ in range(3)]
+        gamma = float(rng.uniform(1.1, 1.67))
+        pr = float(np.exp(rng.uniform(np.log(0.01), 0.0)))
+        rr = float(np.exp(rng.uniform(np.log(0.05), 0.0)))
+        c = float(rng.uniform(0.1, 0.5))
+        grids.append((n[0] + 2, n[1] + 2, n[2] + 2, gamma, 1.0 / n[0], 1.0 / n[1], 1.0 / n[2]))
+        ics.append((c, rr, pr))
+    return grids, ics
+
+
+def oracle_grid(O, grid, ic, steps, cfl=0.4):
+    n0, n1, n2, gamma, dx0, dx1, dx2 = grid
+    c, rr, pr = ic
+    prim = O.init_step(n0, n1, n2, (dx0, dx1, dx2), c, rr, pr, 1.0, 1.0)
+    cons = O.prim_to_cons(prim, gamma)
+    t = O.simulate(prim, cons, gamma, (dx0, dx1, dx2), cfl, steps)
+    return prim, cons, t
+
+
+def test_batch_grids_match_oracle(cuda, euler, oracle_lib):
+    grids, ics = draw_batch(5)
+    steps = 12
+    with euler.Batch(grids, cfl=0.4) as b:
+        for g, (c, rr, pr) in enumerate(ics):
+            b.init_step(g, c, rr, pr)
+        b.advance(steps)
+        assert b.status() == 0
+        for g in range(len(grids)):
+            prim, cons = b.state_numpy(g)
+            pref, cref, tref = oracle_grid(oracle_lib, grids[g], ics[g], steps)
+            t, _, st = b.time(g)
+            assert st == steps
+            assert abs(t - tref) <= 1e-12 * tref, g
+            errs = rel_linf(cons, cref) + rel_linf(prim, pref)
+            assert max(errs) <= 1e-11, (g, errs)
+
+
+def test_autotuned_tiling_is_bit_identical(cuda, euler):
+    grids, ics = draw_batch(9, sizes=(24, 48, 32), ngrids=5)
+    out = []
+    for tune in (False, True):
+        with euler.Batch(grids, cfl=0.4) as b:
+            for g, (c, rr, pr) in enumerate(ics):
+                b.init_step(g, c, rr, pr)
+            if tune:
+                choice = b.autotune(trial_steps=1)
+                assert choice["kchunk"] in (8, 16, 32, 64)
+                assert choice["tile"] in ((32, 8), (16, 8), (16, 16))
+            b.advance(7)
+            out.append([b.state_numpy(g) for g in range(len(grids))])
+    for g in range(len(grids)):
+        assert np.array_equal(out[0][g][0], out[1][g][0]) and np.array_equal(out[0][g][1], out[1][g][1])
+
+
+def test_batch_equals_single_grid_simulation(cuda, euler):
+    grid = (34, 26, 50, 1.3, 1 / 32, 1 / 24, 1 / 48)
+    with euler.Batch([grid, (26, 26, 26, 1.5, 1 / 24, 1 / 24, 1 / 24)], cfl=0.4) as b:
+        b.init_step(0, 0.3, 0.2, 0.05)
+        b.init_step(1, 0.4, 0.5, 0.5)
+        b.advance(9)
+        pb, cb = b.state_numpy(0)
+        tb = b.time(0)
+    import oracle as O
+
+    prim0 = O.init_step(34, 26, 50, grid[4:], 0.3, 0.2, 0.05, 1.0, 1.0)
+    with euler.Simulation(34, 26, 50, 1.3, grid[4:], 0.4) as s:
+        s.set_prim(prim0)
+        s.advance(9)
+        ps, cs = s.state_numpy()
+        ts = s.time()
+    assert np.array_equal(pb, ps) and np.array_equal(cb, cs)
+    assert tb[0] == ts[0]
+
+
+def test_batch_fp32c_tracks_fp64(cuda, euler):
+    grids, ics = draw_batch(3, sizes=(32, 48), ngrids=4)
+    res = {}
+    for precision in ("f64", "f32c"):
+        with euler.Batch(grids, cfl=0.4, precision=precision) as b:
+            for g, (c, rr, pr) in enumerate(ics):
+                b.init_step(g, c, rr, pr)
+            b.advance(20)
+            assert b.status() == 0
+            res[precision] = [b.state_numpy(g)[1][0] for g in range(len(grids))]
+    for g in range(len(grids)):
+        a, ref = res["f32c"][g][1:-1, 1:-1, 1:-1], res["f64"][g][1:-1, 1:-1, 1:-1]
+        assert np.abs(a - ref).sum() / np.abs(ref).sum() < 1e-6
+
+
+def test_batch_rejects_bad_input(cuda, euler):
+    with pytest.raises(euler.EulerError):
+        euler.Batch([(10, 10, 10, 0.9, 0.1, 0.1, 0.1)])
+    with euler.Batch([(10, 10, 10, 1.4, 0.1, 0.1, 0.1)]) as b:
+        with pytest.raises(euler.EulerError):
+            b.advance(1)  # nothing loaded
+        with pytest.raises(euler.EulerError):
+            b.init_step(3, 0.2, 1, 1)  # grid index out of range
