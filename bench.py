@@ -20,6 +20,10 @@ Reported:
              cons_to_prim, time_step, godunov), CUDA-event timed
   cpu_baseline  the CPU oracle (C restatement of the reference operators,
              OpenMP on all host cores) on a bounded slab of the same workload
+  adjoint    the differentiation workload (128^3 implosion with density
+             noise, 400 fixed-dt steps, checkpoints every 20): reverse-step
+             and recompute cost per step against a plain forward step, and
+             central differences of the FP64 solver against the gradient
 
 `--impl reference` times the reference's CPU implementation instead (the
 oracle port; the reference's own sources are not present where this runs).
@@ -73,6 +77,13 @@ def parse():
                     help="implosion, FP32 states vs the plain FP64 run (L1/Linf of rho, p, |u|); prints its own JSON")
     ap.add_argument("--study-n", type=int, nargs="+", default=[512, 768])
     ap.add_argument("--study-steps", type=int, default=1000)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-study", action="store_true",
+                    help="only the differentiation workload, with --adj-dirs central-difference directions")
+    ap.add_argument("--adj-n", type=int, default=128)
+    ap.add_argument("--adj-steps", type=int, default=400)
+    ap.add_argument("--adj-every", type=int, default=20)
+    ap.add_argument("--adj-dirs", type=int, default=4)
     return ap.parse_args()
 
 
@@ -321,6 +332,116 @@ def run_precision_study(args):
     return 0
 
 
+def implode_noise_device(torch, E, nx, sigma=1e-3, seed=0):
+    """The differentiation workload's initial state: init_implode on an nx^3
+    interior (ghosts included), rho += N(0, sigma^2) in every cell (numpy
+    PCG64, seeded)."""
+    import numpy as np
+
+    n = nx + 2
+    prim = E.init_implode(n, n, n, (1.0 / nx,) * 3)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    prim[0] += torch.from_numpy(rng.normal(0.0, sigma, size=(n, n, n))).to(prim.device)
+    return prim
+
+
+def box_weight_device(torch, nx):
+    """J's weight: dv on cells whose centres ((i-1)+1/2)/nx lie in [0.4, 0.6]^3."""
+    n = nx + 2
+    x = (torch.arange(n, dtype=torch.float64) - 1 + 0.5) / nx
+    inside = ((x >= 0.4) & (x <= 0.6)).to(torch.float64)
+    w = inside[:, None, None] * inside[None, :, None] * inside[None, None, :] / nx ** 3
+    return w.cuda()
+
+
+def run_adjoint_leg(torch, E, stream, args, ndirs):
+    """Differentiation workload: gradient of J = sum_box rho(T) dv with respect
+    to the initial rho and p (128^3 implosion with density noise, 400 steps at
+    the forward pass's CFL dt sequence held fixed, checkpoints every 20 steps),
+    its cost against a plain forward step, and central differences
+    (eps = 1e-6) of the FP64 solver along seeded random (rho, p) directions."""
+    import numpy as np
+
+    nx, nsteps, every = args.adj_n, args.adj_steps, args.adj_every
+    n = nx + 2
+    dx = (1.0 / nx,) * 3
+    prim0 = implode_noise_device(torch, E, nx, seed=0)
+    w = box_weight_device(torch, nx)
+    # plain fused forward step at this size, device-resident
+    with E.Simulation(n, n, n, GAMMA, dx, CFL, stream=stream) as sim:
+        sim.set_prim(prim0)
+        sim.advance(3)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        sim.advance(100)
+        e.record(stream)
+        e.synchronize()
+        fwd_step_ms = s.elapsed_time(e) / 100
+    adj = E.Adjoint(n, n, n, nsteps, gamma=GAMMA, dx=dx, cfl=CFL, checkpoint_every=every, stream=stream)
+    out = torch.empty_like(prim0)
+    adj.forward(prim0, out=out)  # CFL steps, recorded
+    dts = adj.dts()
+    adj.forward(prim0, dts=dts, out=out)  # the same steps at the fixed sequence (no per-step dt reads)
+    gT = torch.zeros_like(prim0)
+    gT[0] = w
+    g0 = torch.empty_like(prim0)
+    adj.backward(gT, g0)  # warm-up
+    t0 = time.perf_counter()
+    adj.backward(gT, g0)
+    wall = time.perf_counter() - t0
+    tm = adj.timing()
+    J = float((out[0] * w).sum())
+    rec = {"workload": f"init_implode {nx}^3 + rho noise N(0,1e-6), {nsteps} steps at fixed CFL dts, "
+                       f"checkpoints every {every}; J = sum over [0.4,0.6]^3 of rho(T) dv",
+           "J": J, "t_final": float(sum(dts)),
+           "forward_step_ms": fwd_step_ms,
+           "forward_pass_ms": tm["forward_ms"],
+           "reverse_step_ms": tm["reverse_ms"] / nsteps,
+           "recompute_step_ms": tm["recompute_ms"] / nsteps,
+           "backward_wall_s": wall}
+    rec["reverse_over_forward"] = rec["reverse_step_ms"] / fwd_step_ms
+    rec["gradient_step_over_forward"] = (rec["reverse_step_ms"] + rec["recompute_step_ms"]) / fwd_step_ms
+    # central differences on the fixed dt sequence
+    eps = 1e-6
+    rng = np.random.default_rng(2024)
+    errs, pairs = [], []
+    with E.Simulation(n, n, n, GAMMA, dx, CFL, stream=stream) as sim:
+        sim.set_dt_sequence(dts)
+        p = torch.empty_like(prim0)
+        for _ in range(ndirs):
+            v = torch.zeros_like(prim0)
+            v[0] = torch.from_numpy(rng.normal(size=(n, n, n))).cuda()
+            v[1] = torch.from_numpy(rng.normal(size=(n, n, n))).cuda()
+            vals = []
+            for sgn in (1.0, -1.0):
+                sim.set_prim((prim0 + sgn * eps * v).contiguous())
+                sim.advance(nsteps)
+                sim.get_state(prim=p)
+                vals.append(float((p[0] * w).sum()))
+            fd = (vals[0] - vals[1]) / (2 * eps)
+            an = float((g0 * v).sum())
+            errs.append(abs(fd - an) / abs(an))
+            pairs.append([an, fd])
+    rec["central_differences"] = {"eps": eps, "directions": ndirs, "max_rel_err": max(errs) if errs else None,
+                                  "rel_errs": errs, "adjoint_vs_fd": pairs}
+    adj.close()
+    return rec
+
+
+def run_adjoint_study(args):
+    import torch
+
+    import euler_gb300 as E
+
+    E.build()
+    E.load()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rec = run_adjoint_leg(torch, E, stream, args, args.adj_dirs)
+    print(json.dumps({"adjoint_study": rec}), flush=True)
+    return 0
+
+
 def draw_batch(ngrids, seed=0):
     """The batched workload: each axis length drawn from {24,32,48,64,96,128}
     (interior cells; dx = 1/n per axis), gamma U[1.1, 1.67], inner/outer
@@ -550,6 +671,11 @@ def run_ours(args):
         del host, out
         _ = np
 
+    adjoint = None
+    if not args.no_adjoint and rank == 0:
+        adjoint = run_adjoint_leg(torch, E, stream, args, args.adj_dirs)
+        torch.cuda.empty_cache()
+
     cpu = None
     if not args.no_cpu and rank == 0:
         cpu = cpu_baseline(n, args.cpu_seconds)
@@ -572,6 +698,7 @@ def run_ours(args):
             "fp32c": fp32c,
             "batch": batch,
             "operators": ops,
+            "adjoint": adjoint,
             "status": status,
             "sim": {"t": t_sim, "steps_taken": nsteps},
         }
@@ -588,6 +715,8 @@ def main():
         return run_reference(args)
     if args.precision_study:
         return run_precision_study(args)
+    if args.adjoint_study:
+        return run_adjoint_study(args)
     return run_ours(args)
 
 

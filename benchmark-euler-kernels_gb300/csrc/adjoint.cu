@@ -1,0 +1,335 @@
+// Reverse mode (adjoint) of the first-order Godunov/HLLC time step.
+//
+// The reference has no adjoint.  What is differentiated is its time step:
+// godunov (euler_operators/godunov.hpp:15-92) with the HLLC flux
+// (euler_operators/hllc.hpp:50-105), then cons_to_prim
+// (euler_operators/cons_to_prim.hpp:7-33), with dt held fixed.  For step n,
+// with state (prim_n, cons_n):
+//   cons_{n+1} = cons_n - dt_n/dv * sum_d ds_d (F_d(c+1/2) - F_d(c-1/2))   interior cells
+//   prim_{n+1} = cons_to_prim(cons_{n+1})                                  every cell
+// Given cbar = dJ/dcons_{n+1}, one reverse step forms
+//   pbar = (d update / d prim_n)^T cbar              the face solves below
+//   dJ/dcons_n  = cbar + cons_to_prim'(prim_n)^T pbar    (n >= 1)
+//   dJ/dprim_0  = pbar + prim_to_cons'(prim_0)^T cbar    (n == 0: the step reads prim_0 itself)
+//
+// Three kernels per reverse step, all FP64:
+//   adj_prep   per cell: sound speed c and its derivatives dc/dp, dc/drho,
+//              total energy, kinetic energy per mass, and the face weight
+//              w = (dt/dv) cbar on interior cells (0 on ghosts, which the
+//              step never updates).
+//   adj_face   per cell, its three upper faces: the HLLC solve recomputed
+//              from prim_n (nothing of the forward solve is stored), then
+//              its transpose applied to g = ds (w_R - w_L).  Each face
+//              stores its left and right halves (5 values each) apart.
+//   adj_gather per cell: the sum of its six face halves -- every cell reads
+//              only its own halves, so there are no atomics -- then the
+//              cons_to_prim or prim_to_cons transpose.
+//
+// Ties.  The HLLC flux is piecewise smooth: it takes min/max of wave-speed
+// estimates and branches on the sign of ustar.  At an exact tie (equal
+// min/max arguments, or ustar == 0 in the subsonic case) the derivative used
+// is the mean of the two one-sided derivatives, which is what a central
+// difference measures.  Ties are common: a gas at rest with uniform pressure
+// and uneven density has un_L == un_R == 0 and ustar == 0 exactly at every
+// face, and stays at rest step after step.  (Where ustar == 0 with both
+// velocities 0, the flux does not depend on the wave speeds to first order,
+// so the only one-sided difference is in the mass flux, rho_L vs rho_R times
+// d ustar; its mean is linear in the perturbation.)
+#include "adjoint_face.cuh"
+#include "kernels.h"
+
+namespace eulr {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+struct AdjParams {
+    Geom g;
+    CBundle<double> prim;
+    CBundle<double> cbar;
+    Bundle<double> out;
+    AdjWork w;
+    double gamma, gm1, inv_gm1;
+    double ds[3];
+    double wscale; // dt / dv
+    int mode;
+};
+
+__device__ __forceinline__ bool interior(Geom const& g, int i, int j, int k)
+{
+    return i >= 1 && i < g.n0 - 1 && j >= 1 && j < g.n1 - 1 && k >= 1 && k < g.n2 - 1;
+}
+
+__device__ __forceinline__ void decode(Geom const& g, long long c, int& i, int& j, int& k)
+{
+    k = static_cast<int>(c / g.s2);
+    long long const r = c - static_cast<long long>(k) * g.s2;
+    j = static_cast<int>(r / g.s1);
+    i = static_cast<int>(r - static_cast<long long>(j) * g.s1);
+}
+
+__global__ void __launch_bounds__(kThreads) adj_prep_kernel(AdjParams p)
+{
+    long long const n = p.g.ncell();
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        double const d = p.prim.f[0][c];
+        double const pr = p.prim.f[1][c];
+        double const u0 = p.prim.f[2][c];
+        double const u1 = p.prim.f[3][c];
+        double const u2 = p.prim.f[4][c];
+        double const R = __drcp_rn(d * pr);
+        double const inv_d = pr * R;
+        double const inv_p = d * R;
+        double const c2 = (p.gamma * pr) * inv_d;
+        double const cs = c2 * rsqrt(c2);
+        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        p.w.derived[0][c] = cs;
+        p.w.derived[1][c] = 0.5 * cs * inv_p;
+        p.w.derived[2][c] = -0.5 * cs * inv_d;
+        p.w.derived[3][c] = pr * p.inv_gm1 + d * ke;
+        p.w.derived[4][c] = ke;
+        int i, j, k;
+        decode(p.g, c, i, j, k);
+        bool const in = interior(p.g, i, j, k);
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            p.w.weight[f][c] = in ? p.wscale * p.cbar.f[f][c] : 0.0;
+        }
+    }
+}
+
+__device__ __forceinline__ FaceSide load_side(AdjParams const& p, long long c, int a)
+{
+    FaceSide s;
+    s.r = p.prim.f[0][c];
+    s.p = p.prim.f[1][c];
+    s.un = p.prim.f[2 + a][c];
+    s.t1 = p.prim.f[2 + (a + 1) % 3][c];
+    s.t2 = p.prim.f[2 + (a + 2) % 3][c];
+    s.c = p.w.derived[0][c];
+    s.cp = p.w.derived[1][c];
+    s.cr = p.w.derived[2][c];
+    s.e = p.w.derived[3][c];
+    s.ke = p.w.derived[4][c];
+    return s;
+}
+
+__device__ __forceinline__ void store_half(AdjParams const& p, int a, int side, long long c, FaceBar const& b)
+{
+    double* const* f = p.w.face + (a * 2 + side) * 5;
+    f[0][c] = b.r;
+    f[1][c] = b.p;
+    f[2 + a][c] = b.un;
+    f[2 + (a + 1) % 3][c] = b.t1;
+    f[2 + (a + 2) % 3][c] = b.t2;
+}
+
+__global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
+{
+    long long const n = p.g.ncell();
+    long long const stride[3] = {1, p.g.s1, p.g.s2};
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int idx[3];
+        decode(p.g, c, idx[0], idx[1], idx[2]);
+        int const ext[3] = {p.g.n0, p.g.n1, p.g.n2};
+#pragma unroll 1
+        for (int a = 0; a < 3; ++a) {
+            int const b = (a + 1) % 3, e = (a + 2) % 3;
+            // the face between c and c + e_a is solved by the step when one side is interior
+            bool const active = idx[a] <= ext[a] - 2 && idx[b] >= 1 && idx[b] <= ext[b] - 2 && idx[e] >= 1 &&
+                                idx[e] <= ext[e] - 2;
+            FaceBar bL, bR;
+            zero(bL);
+            zero(bR);
+            if (active) {
+                long long const cr = c + stride[a];
+                double g[5];
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    g[f] = p.ds[a] * (p.w.weight[f][cr] - p.w.weight[f][c]);
+                }
+                FaceSide const L = load_side(p, c, a);
+                FaceSide const R = load_side(p, cr, a);
+                hllc_bar(L, R, g[0], g[1], g[2 + a], g[2 + b], g[2 + e], p.inv_gm1, bL, bR);
+            }
+            store_half(p, a, 0, c, bL);
+            store_half(p, a, 1, c, bR);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) adj_gather_kernel(AdjParams p)
+{
+    long long const n = p.g.ncell();
+    long long const stride[3] = {1, p.g.s1, p.g.s2};
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int idx[3];
+        decode(p.g, c, idx[0], idx[1], idx[2]);
+        double pb[5];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            double s = 0.0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                s += p.w.face[(a * 2 + 0) * 5 + f][c]; // faces where this cell is the left side
+                if (idx[a] >= 1) {
+                    s += p.w.face[(a * 2 + 1) * 5 + f][c - stride[a]]; // ... and the right side
+                }
+            }
+            pb[f] = s;
+        }
+        double const d = p.prim.f[0][c];
+        double const u0 = p.prim.f[2][c], u1 = p.prim.f[3][c], u2 = p.prim.f[4][c];
+        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        if (p.mode == kAdjStep) {
+            // cons_to_prim: p = (gamma-1)(e - |m|^2/(2d)), u = m/d
+            double const inv_d = __drcp_rn(d);
+            double const gp = pb[1] * p.gm1;
+            double const c0 = p.cbar.f[0][c], c1 = p.cbar.f[1][c];
+            double const c2 = p.cbar.f[2][c], c3 = p.cbar.f[3][c], c4 = p.cbar.f[4][c];
+            p.out.f[0][c] = c0 + pb[0] + gp * ke - inv_d * (pb[2] * u0 + pb[3] * u1 + pb[4] * u2);
+            p.out.f[1][c] = c1 + gp;
+            p.out.f[2][c] = c2 + pb[2] * inv_d - gp * u0;
+            p.out.f[3][c] = c3 + pb[3] * inv_d - gp * u1;
+            p.out.f[4][c] = c4 + pb[4] * inv_d - gp * u2;
+        } else if (p.mode == kAdjInitial) {
+            // prim_to_cons: e = p/(gamma-1) + d |u|^2 / 2, m = d u
+            double const c0 = p.cbar.f[0][c], c1 = p.cbar.f[1][c];
+            double const c2 = p.cbar.f[2][c], c3 = p.cbar.f[3][c], c4 = p.cbar.f[4][c];
+            p.out.f[0][c] = pb[0] + c0 + c1 * ke + c2 * u0 + c3 * u1 + c4 * u2;
+            p.out.f[1][c] = pb[1] + c1 * p.inv_gm1;
+            p.out.f[2][c] = pb[2] + (c1 * u0 + c2) * d;
+            p.out.f[3][c] = pb[3] + (c1 * u1 + c3) * d;
+            p.out.f[4][c] = pb[4] + (c1 * u2 + c4) * d;
+        } else {
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                p.out.f[f][c] = pb[f];
+            }
+        }
+    }
+}
+
+// cbar (+)= cons_to_prim'(prim)^T pbar
+__global__ void __launch_bounds__(kThreads) c2p_bar_kernel(CBundle<double> prim, CBundle<double> pbar,
+                                                          Bundle<double> cbar, long long n, double gm1, int acc)
+{
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        double const d = prim.f[0][c];
+        double const u0 = prim.f[2][c], u1 = prim.f[3][c], u2 = prim.f[4][c];
+        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        double const inv_d = __drcp_rn(d);
+        double const b0 = pbar.f[0][c], b2 = pbar.f[2][c], b3 = pbar.f[3][c], b4 = pbar.f[4][c];
+        double const gp = pbar.f[1][c] * gm1;
+        double r[5];
+        r[0] = b0 + gp * ke - inv_d * (b2 * u0 + b3 * u1 + b4 * u2);
+        r[1] = gp;
+        r[2] = b2 * inv_d - gp * u0;
+        r[3] = b3 * inv_d - gp * u1;
+        r[4] = b4 * inv_d - gp * u2;
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            cbar.f[f][c] = acc ? cbar.f[f][c] + r[f] : r[f];
+        }
+    }
+}
+
+// pbar (+)= prim_to_cons'(prim)^T cbar
+__global__ void __launch_bounds__(kThreads) p2c_bar_kernel(CBundle<double> prim, CBundle<double> cbar,
+                                                          Bundle<double> pbar, long long n, double inv_gm1, int acc)
+{
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        double const d = prim.f[0][c];
+        double const u0 = prim.f[2][c], u1 = prim.f[3][c], u2 = prim.f[4][c];
+        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        double const c0 = cbar.f[0][c], c1 = cbar.f[1][c], c2 = cbar.f[2][c], c3 = cbar.f[3][c];
+        double const c4 = cbar.f[4][c];
+        double r[5];
+        r[0] = c0 + c1 * ke + c2 * u0 + c3 * u1 + c4 * u2;
+        r[1] = c1 * inv_gm1;
+        r[2] = (c1 * u0 + c2) * d;
+        r[3] = (c1 * u1 + c3) * d;
+        r[4] = (c1 * u2 + c4) * d;
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            pbar.f[f][c] = acc ? pbar.f[f][c] + r[f] : r[f];
+        }
+    }
+}
+
+int blocks_for(long long n, int sms, int per_sm)
+{
+    long long const b = (n + kThreads - 1) / kThreads;
+    long long const cap = static_cast<long long>(sms) * per_sm;
+    return static_cast<int>(b < 1 ? 1 : (b < cap ? b : cap));
+}
+
+size_t pad_field(long long n) { return (static_cast<size_t>(n) * sizeof(double) + 255) & ~static_cast<size_t>(255); }
+
+} // namespace
+
+size_t adjoint_workspace_bytes(long long ncell) { return pad_field(ncell) * kAdjWorkFields; }
+
+AdjWork adjoint_workspace(void* base, long long ncell)
+{
+    AdjWork w{};
+    size_t const field = pad_field(ncell);
+    char* p = static_cast<char*>(base);
+    for (int f = 0; f < 30; ++f, p += field) {
+        w.face[f] = reinterpret_cast<double*>(p);
+    }
+    for (int f = 0; f < 5; ++f, p += field) {
+        w.derived[f] = reinterpret_cast<double*>(p);
+    }
+    for (int f = 0; f < 5; ++f, p += field) {
+        w.weight[f] = reinterpret_cast<double*>(p);
+    }
+    return w;
+}
+
+cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> out, int mode, Geom g,
+                                double gamma, double dx0, double dx1, double dx2, double dt, AdjWork const& w, int sms,
+                                cudaStream_t s)
+{
+    AdjParams p;
+    p.g = g;
+    p.prim = prim;
+    p.cbar = cbar;
+    p.out = out;
+    p.w = w;
+    p.gamma = gamma;
+    p.gm1 = gamma - 1.0;
+    p.inv_gm1 = 1.0 / (gamma - 1.0);
+    p.ds[0] = dx1 * dx2; // uniform_mesh.hpp:33-46
+    p.ds[1] = dx2 * dx0;
+    p.ds[2] = dx0 * dx1;
+    p.wscale = dt / (dx0 * dx1 * dx2);
+    p.mode = mode;
+    long long const n = g.ncell();
+    adj_prep_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    adj_face_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    adj_gather_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cons_to_prim_adjoint(CBundle<double> prim, CBundle<double> pbar, Bundle<double> cbar,
+                                        int accumulate, long long n, double gamma, int sms, cudaStream_t s)
+{
+    c2p_bar_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(prim, pbar, cbar, n, gamma - 1.0, accumulate);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prim_to_cons_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> pbar,
+                                        int accumulate, long long n, double gamma, int sms, cudaStream_t s)
+{
+    p2c_bar_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(prim, cbar, pbar, n, 1.0 / (gamma - 1.0), accumulate);
+    return cudaGetLastError();
+}
+
+} // namespace eulr

@@ -1,0 +1,187 @@
+// Transposed HLLC flux of one face: the arithmetic of the reverse step
+// (adjoint.cu), in a header that also compiles as plain host C++ so that the
+// CPU tests can check it against the host tangent-linear model.
+//
+// The flux differentiated is hllc::operator() of euler_operators/hllc.hpp:50-105.
+// At exact ties (equal min/max arguments, ustar == 0 in the subsonic case)
+// the derivative is the mean of the two one-sided derivatives.
+#pragma once
+
+#if defined(__CUDACC__)
+#define EULR_ADJ_FN __host__ __device__ __forceinline__
+#else
+#define EULR_ADJ_FN inline
+#endif
+
+namespace eulr {
+
+// Correctly rounded reciprocal (the device instruction sequence on the GPU).
+EULR_ADJ_FN double adj_rcp(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return __drcp_rn(x);
+#else
+    return 1.0 / x;
+#endif
+}
+
+// One side of a face in the face frame: normal velocity un, tangential t1, t2.
+struct FaceSide {
+    double r, p, un, t1, t2;
+    double c, cp, cr; // sound speed, dc/dp, dc/drho
+    double e, ke;     // total energy per volume, kinetic energy per mass
+};
+
+struct FaceBar {
+    double r, p, un, t1, t2;
+};
+
+EULR_ADJ_FN void zero(FaceBar& b) { b.r = b.p = b.un = b.t1 = b.t2 = 0.0; }
+
+// Subsonic star-state branch of side Q (hllc.hpp:78-102 with S = S_Q, q = Q):
+// adds its transposed contribution for the cotangent (gd, ge, gn, gt1, gt2)
+// to gus (d/d ustar), gps (d/d pstar) and bq, and returns d/d S_Q.
+EULR_ADJ_FN double star_branch_bar(FaceSide const& q, double S, double a, double iY, double ustar,
+                                                  double pstar, double gd, double ge, double gn, double gt1,
+                                                  double gt2, double inv_gm1, double& gus, double& gps, FaceBar& bq)
+{
+    // forward: ratio = (S - un)/(S - ustar), d_o = ratio rho, etot_o = ratio e + X/(S - ustar),
+    // X = pstar ustar - p un; fluxes m = d_o ustar; (m, (etot_o + pstar) ustar, m ustar + pstar, m t1, m t2)
+    double const r = a * iY;
+    double const X = pstar * ustar - q.p * q.un;
+    double const Xy = X * iY;
+    double const d_o = r * q.r;
+    double const eo = r * q.e + Xy;
+    double const m = d_o * ustar;
+    double const gm = gd + gn * ustar + gt1 * q.t1 + gt2 * q.t2;
+    gus += gn * m + ge * (eo + pstar) + gm * d_o;
+    gps += gn + ge * ustar;
+    double const gE = ge * ustar;          // d/d etot_o
+    double const gdo = gm * ustar;         // d/d d_o
+    double const gr = gdo * q.r + gE * q.e; // d/d ratio
+    double const geq = gE * r;             // d/d e (side total energy)
+    double const gX = gE * iY;
+    double const gY = -(gE * Xy + gr * r) * iY; // d/d (S - ustar)
+    double const ga = gr * iY;                  // d/d (S - un)
+    gps += gX * ustar;
+    gus += gX * pstar - gY;
+    bq.r += gdo * r + geq * q.ke;
+    bq.p += geq * inv_gm1 - gX * q.un;
+    bq.un += geq * (q.r * q.un) - gX * q.p - ga;
+    bq.t1 += gt1 * m + geq * (q.r * q.t1);
+    bq.t2 += gt2 * m + geq * (q.r * q.t2);
+    return gY + ga;
+}
+
+// Transposed HLLC flux of one face (hllc.hpp:50-105): given the cotangent of
+// the face flux in the face frame (gd, ge, gn, gt1, gt2), adds the cotangents
+// of both sides' primitive states to bL and bR.
+EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double gd, double ge, double gn, double gt1,
+                                         double gt2, double inv_gm1, FaceBar& bL, FaceBar& bR)
+{
+    // S_L = min(un_L, un_R) - max(c_L, c_R), S_R = max(un_L, un_R) + max(c_L, c_R)
+    bool const u_lt = L.un < R.un;
+    bool const u_gt = R.un < L.un;
+    bool const c_lt = L.c < R.c;
+    bool const c_gt = R.c < L.c;
+    double const umin = u_gt ? R.un : L.un;
+    double const umax = u_lt ? R.un : L.un;
+    double const cmax = c_lt ? R.c : L.c;
+    double const SL = umin - cmax;
+    double const SR = umax + cmax;
+    double const aL = SL - L.un;
+    double const aR = SR - R.un;
+    double const rcL = L.r * aL;
+    double const rcR = R.r * aR;
+    double const num = (R.p - L.p) + rcL * L.un - rcR * R.un;
+    double const den = rcL - rcR; // rcL <= 0 <= rcR: den < 0, so ustar > 0 exactly when num < 0
+    bool const left = num < 0.0;
+    bool const tie = num == 0.0;
+
+    if (SL > 0.0 || SR < 0.0) {
+        // S_L * S_R > 0: the flux is the upwind side's physical flux (ustar > 0 picks L)
+        FaceSide const& q = left ? L : R;
+        FaceBar& bq = left ? bL : bR;
+        double const m = q.r * q.un;
+        double const gm = gd + gn * q.un + gt1 * q.t1 + gt2 * q.t2;
+        double const geq = ge * q.un;
+        bq.un += gn * m + ge * (q.e + q.p) + gm * q.r + geq * (q.r * q.un);
+        bq.r += gm * q.un + geq * q.ke;
+        bq.p += gn + ge * q.un + geq * inv_gm1;
+        bq.t1 += gt1 * m + geq * (q.r * q.t1);
+        bq.t2 += gt2 * m + geq * (q.r * q.t2);
+        return;
+    }
+
+    // One reciprocal gives 1/den and 1/(S - ustar): with Z = S den - num,
+    // S - ustar = Z/den, so 1/den = Z R and 1/(S - ustar) = den^2 R for R = 1/(den Z).
+    double const S0 = left ? SL : SR;
+    double const Z = S0 * den - num;
+    double const Rr = adj_rcp(den * Z);
+    double const inv_den = Z * Rr;
+    double const iY0 = (den * den) * Rr;
+    double const ustar = num * inv_den;
+    double const pstar = 0.5 * (L.p + R.p + rcL * (ustar - L.un) + rcR * (ustar - R.un));
+
+    double gus = 0.0, gps = 0.0, gSL = 0.0, gSR = 0.0;
+    double const w = tie ? 0.5 : 1.0;
+    double const hd = w * gd, he = w * ge, hn = w * gn, h1 = w * gt1, h2 = w * gt2;
+    if (left) {
+        gSL += star_branch_bar(L, SL, aL, iY0, ustar, pstar, hd, he, hn, h1, h2, inv_gm1, gus, gps, bL);
+    } else {
+        gSR += star_branch_bar(R, SR, aR, iY0, ustar, pstar, hd, he, hn, h1, h2, inv_gm1, gus, gps, bR);
+    }
+    if (tie) { // the forward took R; add the mean with the L branch
+        double const iY1 = adj_rcp(SL - ustar);
+        gSL += star_branch_bar(L, SL, aL, iY1, ustar, pstar, hd, he, hn, h1, h2, inv_gm1, gus, gps, bL);
+    }
+
+    // pstar = (p_L + p_R + rc_L (ustar - un_L) + rc_R (ustar - un_R)) / 2
+    double const h = 0.5 * gps;
+    bL.p += h;
+    bR.p += h;
+    double grcL = h * (ustar - L.un);
+    double grcR = h * (ustar - R.un);
+    gus += h * (rcL + rcR);
+    bL.un -= h * rcL;
+    bR.un -= h * rcR;
+    // ustar = num / den
+    double const gnum = gus * inv_den;
+    double const gden = -gnum * ustar;
+    bR.p += gnum;
+    bL.p -= gnum;
+    grcL += gnum * L.un + gden;
+    grcR -= gnum * R.un + gden;
+    bL.un += gnum * rcL;
+    bR.un -= gnum * rcR;
+    // rc = rho (S - un)
+    bL.r += grcL * aL;
+    bR.r += grcR * aR;
+    double const gaL = grcL * L.r;
+    double const gaR = grcR * R.r;
+    gSL += gaL;
+    gSR += gaR;
+    bL.un -= gaL;
+    bR.un -= gaR;
+    // S_L = umin - cmax, S_R = umax + cmax
+    if (u_lt) {
+        bL.un += gSL;
+        bR.un += gSR;
+    } else if (u_gt) {
+        bR.un += gSL;
+        bL.un += gSR;
+    } else {
+        double const hs = 0.5 * (gSL + gSR);
+        bL.un += hs;
+        bR.un += hs;
+    }
+    double const gc = gSR - gSL;
+    double const gcL = c_lt ? 0.0 : (c_gt ? gc : 0.5 * gc);
+    double const gcR = gc - gcL;
+    bL.p += gcL * L.cp;
+    bL.r += gcL * L.cr;
+    bR.p += gcR * R.cp;
+    bR.r += gcR * R.cr;
+}
+
+} // namespace eulr

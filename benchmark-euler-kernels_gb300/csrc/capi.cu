@@ -324,6 +324,54 @@ int godunov_impl(PB prim, CB cons, int n0, int n1, int n2, T gamma, T dx0, T dx1
     return EULR_SUCCESS;
 }
 
+// Rejects overlap between any output array and any input array (inputs may
+// overlap one another).
+int check_out_disjoint(const void* const* out, int nout, const void* const* in, int nin, size_t bytes,
+                       const char* what)
+{
+    for (int a = 0; a < nout; ++a) {
+        for (int b = 0; b < nin; ++b) {
+            auto const pa = reinterpret_cast<std::uintptr_t>(out[a]);
+            auto const pb = reinterpret_cast<std::uintptr_t>(in[b]);
+            if (pa < pb + bytes && pb < pa + bytes) {
+                return fail(EULR_ERR_INVALID_ARGUMENT, "%s: output %d overlaps input %d", what, a, b);
+            }
+        }
+    }
+    return EULR_SUCCESS;
+}
+
+// The two pointwise transposes: kind 0 = cons_to_prim (out is cons_bar), 1 = prim_to_cons (out is prim_bar).
+int pointwise_adjoint_impl(int kind, const void* const* prim, const void* const* in_bar, void* const* out_bar, int n0,
+                           int n1, int n2, double gamma, int accumulate, cudaStream_t s)
+{
+    EULR_TRY(check_dims(n0, n1, n2));
+    EULR_TRY(check_fields<double>(prim, 5, "prim"));
+    EULR_TRY(check_fields<double>(in_bar, 5, "input adjoint"));
+    EULR_TRY(check_fields<double>(out_bar, 5, "output adjoint"));
+    EULR_TRY(check_gamma(gamma));
+    long long const n = static_cast<long long>(n0) * n1 * n2;
+    size_t const bytes = static_cast<size_t>(n) * sizeof(double);
+    EULR_TRY(check_disjoint(out_bar, 5, bytes, "adjoint output"));
+    const void* ins[10];
+    std::memcpy(ins, prim, 5 * sizeof(void*));
+    std::memcpy(ins + 5, in_bar, 5 * sizeof(void*));
+    EULR_TRY(check_out_disjoint(out_bar, 5, ins, 10, bytes, "adjoint"));
+    int sms = 0;
+    EULR_TRY(current_sms(&sms));
+    CBundle<double> pv, iv;
+    Bundle<double> ov;
+    for (int f = 0; f < 5; ++f) {
+        pv.f[f] = static_cast<const double*>(prim[f]);
+        iv.f[f] = static_cast<const double*>(in_bar[f]);
+        ov.f[f] = static_cast<double*>(out_bar[f]);
+    }
+    cudaError_t const e = kind == 0 ? launch_cons_to_prim_adjoint(pv, iv, ov, accumulate, n, gamma, sms, s)
+                                    : launch_prim_to_cons_adjoint(pv, iv, ov, accumulate, n, gamma, sms, s);
+    EULR_CUDA_TRY(e, "adjoint launch");
+    return EULR_SUCCESS;
+}
+
 } // namespace
 
 namespace eulr {
@@ -427,6 +475,77 @@ int eulr_godunov_devdt_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int 
         return fail(EULR_ERR_INVALID_ARGUMENT, "dt_dev is NULL");
     }
     return godunov_impl<double>(prim, cons, n0, n1, n2, gamma, dx0, dx1, dx2, 0.0, dt_dev, cfl, stream);
+}
+
+size_t eulr_godunov_adjoint_workspace_bytes(int n0, int n1, int n2)
+{
+    if (n0 < 1 || n1 < 1 || n2 < 1 || static_cast<long long>(n0) * n1 * n2 > INT_MAX) {
+        return 0;
+    }
+    return adjoint_workspace_bytes(static_cast<long long>(n0) * n1 * n2);
+}
+
+int eulr_godunov_adjoint_f64(eulr_prim_cf64 prim, eulr_cons_cf64 cons_bar, eulr_prim_f64 prim_bar, int n0, int n1,
+                             int n2, double gamma, double dx0, double dx1, double dx2, double dt, void* workspace,
+                             size_t workspace_bytes, eulr_stream_t stream)
+{
+    EULR_TRY(check_dims(n0, n1, n2));
+    EULR_TRY(check_fields<double>(reinterpret_cast<const void* const*>(&prim), 5, "prim"));
+    EULR_TRY(check_fields<double>(reinterpret_cast<const void* const*>(&cons_bar), 5, "cons_bar"));
+    EULR_TRY(check_fields<double>(reinterpret_cast<const void* const*>(&prim_bar), 5, "prim_bar"));
+    EULR_TRY(check_gamma(gamma));
+    EULR_TRY(check_dx(dx0, dx1, dx2));
+    if (!std::isfinite(dt)) {
+        return fail(EULR_ERR_INVALID_VALUE, "dt must be finite");
+    }
+    long long const n = static_cast<long long>(n0) * n1 * n2;
+    size_t const need = adjoint_workspace_bytes(n);
+    if (workspace == nullptr || workspace_bytes < need) {
+        return fail(EULR_ERR_INVALID_ARGUMENT, "workspace of %zu bytes needed (got %zu)", need,
+                    workspace == nullptr ? static_cast<size_t>(0) : workspace_bytes);
+    }
+    if (reinterpret_cast<std::uintptr_t>(workspace) % 256 != 0) {
+        return fail(EULR_ERR_MISALIGNED, "workspace must be 256-byte aligned");
+    }
+    size_t const bytes = static_cast<size_t>(n) * sizeof(double);
+    const void* outs[5];
+    std::memcpy(outs, &prim_bar, sizeof(outs));
+    EULR_TRY(check_disjoint(outs, 5, bytes, "godunov adjoint output"));
+    const void* ins[10];
+    std::memcpy(ins, &prim, 5 * sizeof(void*));
+    std::memcpy(ins + 5, &cons_bar, 5 * sizeof(void*));
+    EULR_TRY(check_out_disjoint(outs, 5, ins, 10, bytes, "godunov adjoint"));
+    auto const ws = reinterpret_cast<std::uintptr_t>(workspace);
+    for (int f = 0; f < 15; ++f) {
+        auto const pf = reinterpret_cast<std::uintptr_t>(f < 10 ? ins[f] : outs[f - 10]);
+        if (pf < ws + need && ws < pf + bytes) {
+            return fail(EULR_ERR_INVALID_ARGUMENT, "godunov adjoint: the workspace overlaps argument array %d", f);
+        }
+    }
+    int sms = 0;
+    EULR_TRY(current_sms(&sms));
+    AdjWork const w = adjoint_workspace(workspace, n);
+    EULR_CUDA_TRY(launch_step_adjoint(to_cbundle<double>(prim), to_cbundle<double>(cons_bar),
+                                      to_bundle<double>(prim_bar), kAdjGodunov, make_geom(n0, n1, n2), gamma, dx0,
+                                      dx1, dx2, dt, w, sms, stream),
+                  "godunov adjoint launch");
+    return EULR_SUCCESS;
+}
+
+int eulr_cons_to_prim_adjoint_f64(eulr_prim_cf64 prim, eulr_prim_cf64 prim_bar, eulr_cons_f64 cons_bar, int n0,
+                                  int n1, int n2, double gamma, int accumulate, eulr_stream_t stream)
+{
+    return pointwise_adjoint_impl(0, reinterpret_cast<const void* const*>(&prim),
+                                  reinterpret_cast<const void* const*>(&prim_bar),
+                                  reinterpret_cast<void* const*>(&cons_bar), n0, n1, n2, gamma, accumulate, stream);
+}
+
+int eulr_prim_to_cons_adjoint_f64(eulr_prim_cf64 prim, eulr_cons_cf64 cons_bar, eulr_prim_f64 prim_bar, int n0,
+                                  int n1, int n2, double gamma, int accumulate, eulr_stream_t stream)
+{
+    return pointwise_adjoint_impl(1, reinterpret_cast<const void* const*>(&prim),
+                                  reinterpret_cast<const void* const*>(&cons_bar),
+                                  reinterpret_cast<void* const*>(&prim_bar), n0, n1, n2, gamma, accumulate, stream);
 }
 
 int eulr_probe_fma_rate(int kind, int iters, double* flops)

@@ -558,6 +558,9 @@ __device__ __forceinline__ TileCtx<T> make_ctx(unsigned char* smem_dyn)
 template <class T>
 __device__ __forceinline__ T dt_over_dv(FluxParams<T> const& p)
 {
+    if (p.dt_seq != nullptr) {
+        return static_cast<T>(p.dt_seq[*p.step_dev] / p.dv);
+    }
     if (p.dt_dev != nullptr) {
         return static_cast<T>((p.cfl * *p.dt_dev) / p.dv);
     }
@@ -761,10 +764,10 @@ __global__ void __launch_bounds__(256) ghost_batch_kernel(const GhostParams<T>* 
 // (time_step.hpp:34-39: min over cells of 1/invdt == 1/max invdt), adds the
 // step just taken to the simulated time and clears the accumulator.
 template <class T>
-__device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time)
+__device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time, const double* dt_seq = nullptr)
 {
     if (add_time) {
-        s->t += static_cast<double>(cfl * static_cast<T>(s->dt));
+        s->t += dt_seq != nullptr ? dt_seq[s->steps] : static_cast<double>(cfl * static_cast<T>(s->dt));
         s->steps += 1;
     }
     T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(s->wmax)));
@@ -774,10 +777,10 @@ __device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time)
 }
 
 template <class T>
-__global__ void finalize_dt_kernel(SimScalars* s, T cfl, int add_time)
+__global__ void finalize_dt_kernel(SimScalars* s, T cfl, int add_time, const double* dt_seq)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        finalize_one(s, cfl, add_time);
+        finalize_one(s, cfl, add_time, dt_seq);
     }
 }
 
@@ -1053,9 +1056,9 @@ cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s)
 }
 
 template <class T>
-cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s)
+cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s, const double* dt_seq)
 {
-    finalize_dt_kernel<T><<<1, 32, 0, s>>>(sc, cfl, add_time);
+    finalize_dt_kernel<T><<<1, 32, 0, s>>>(sc, cfl, add_time, dt_seq);
     return cudaGetLastError();
 }
 
@@ -1068,7 +1071,7 @@ template cudaError_t launch_flux<double>(FluxParams<double>, TmaMaps const*, int
 template cudaError_t launch_flux<float>(FluxParams<float>, TmaMaps const*, int, int, int, cudaStream_t);
 template cudaError_t launch_ghost_shell<double>(GhostParams<double>, int, cudaStream_t);
 template cudaError_t launch_ghost_shell<float>(GhostParams<float>, int, cudaStream_t);
-template cudaError_t launch_finalize_dt<double>(SimScalars*, double, int, cudaStream_t);
-template cudaError_t launch_finalize_dt<float>(SimScalars*, float, int, cudaStream_t);
+template cudaError_t launch_finalize_dt<double>(SimScalars*, double, int, cudaStream_t, const double*);
+template cudaError_t launch_finalize_dt<float>(SimScalars*, float, int, cudaStream_t, const double*);
 
 } // namespace eulr

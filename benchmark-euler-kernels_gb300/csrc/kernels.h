@@ -6,6 +6,8 @@
 
 #include "euler_device.cuh"
 
+struct eulr_sim;
+
 namespace eulr {
 
 constexpr int kModeGodunov = 0; // per-operator godunov: cons updated in place from prim
@@ -48,6 +50,8 @@ struct FluxParams {
     T dtodv;             // dt/dv when dt_dev is null
     const double* dt_dev; // if set: dt/dv = (cfl * *dt_dev) / dv, evaluated in double
     double cfl;
+    const double* dt_seq;       // if set: step n uses dt = dt_seq[n] (a fixed sequence, CFL not applied)
+    const long long* step_dev;  // the step index n (SimScalars::steps)
     CBundle<T> lo_in;    // compensated FP32 state: low words of cons (comp == 2)
     Bundle<T> lo_out;
     T invdx0, invdx1, invdx2;
@@ -122,7 +126,7 @@ cudaError_t launch_finalize_batch(SimScalars* sc, int ngrids, T cfl, int add_tim
 template <class T>
 cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s);
 template <class T>
-cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s);
+cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s, const double* dt_seq = nullptr);
 
 cudaError_t launch_fma_probe(int kind, int blocks, int iters, float* sink, cudaStream_t s);
 template <class T>
@@ -131,5 +135,44 @@ cudaError_t launch_state_to_f32(CBundle<double> prim, CBundle<double> cons, Bund
                                 long long n, double gamma, int fp32_cons, int sms, cudaStream_t s);
 cudaError_t launch_state_from_f32(CBundle<float> hi, CBundle<float> lo, Bundle<double> prim, Bundle<double> cons,
                                   long long n, double gamma, int sms, cudaStream_t s);
+
+// Reverse mode of the time step (adjoint.cu).  Output of launch_step_adjoint
+// by mode, for the state (prim, cons) a step starts from and cbar = dJ/d(cons
+// the step produces):
+constexpr int kAdjStep = 0;    // out = dJ/dcons: cbar + cons_to_prim'(prim)^T pbar
+constexpr int kAdjInitial = 1; // out = dJ/dprim of a step that reads prim itself: pbar + prim_to_cons'(prim)^T cbar
+constexpr int kAdjGodunov = 2; // out = pbar = (d godunov / d prim)^T cbar
+constexpr int kAdjWorkFields = 40;
+
+// Workspace of the reverse step: the left/right halves of each cell's three
+// upper faces (index (axis*2 + side)*5 + prim field), per-cell sound speed
+// data and energies, and the weighted cotangent.
+struct AdjWork {
+    double* face[30];
+    double* derived[5]; // c, dc/dp, dc/drho, total energy, kinetic energy per mass
+    double* weight[5];  // (dt/dv) cbar on interior cells, 0 on ghosts
+};
+
+size_t adjoint_workspace_bytes(long long ncell);
+AdjWork adjoint_workspace(void* base, long long ncell);
+cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> out, int mode, Geom g,
+                                double gamma, double dx0, double dx1, double dx2, double dt, AdjWork const& w, int sms,
+                                cudaStream_t s);
+cudaError_t launch_cons_to_prim_adjoint(CBundle<double> prim, CBundle<double> pbar, Bundle<double> cbar,
+                                        int accumulate, long long n, double gamma, int sms, cudaStream_t s);
+cudaError_t launch_prim_to_cons_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> pbar,
+                                        int accumulate, long long n, double gamma, int sms, cudaStream_t s);
+
+// Raw state of an FP64 simulation, for the checkpointed adjoint.  The fields
+// are, in order, prim (5), cons (5) and the sound speed (1) of the current
+// copy.  sim_snapshot copies the first nfields of them to device memory (on
+// the simulation's stream, asynchronously); sim_restore loads all 11 into the
+// first copy and sets the step counter (which indexes a fixed dt sequence).
+int sim_snapshot(eulr_sim* s, double* const* dst, int nfields);
+// Records msg as the last error (eulr_last_error) and returns status.
+int sim_fail(int status, const char* msg);
+int sim_restore(eulr_sim* s, const double* const* src, long long step);
+// The stream the simulation's work runs on (its own when created with NULL).
+cudaStream_t sim_stream(eulr_sim* s);
 
 } // namespace eulr

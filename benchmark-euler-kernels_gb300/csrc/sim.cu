@@ -99,6 +99,9 @@ struct eulr_sim {
     TmaMaps maps[2] = {}; // descriptors of copy 0 and copy 1 as step input
     bool loaded = false;
     cudaGraphExec_t graph = nullptr;
+    double* dt_seq = nullptr;  // device copy of a fixed dt sequence (owned), or null
+    long long dt_seq_len = 0;
+    long long host_steps = 0;  // steps taken since the state was loaded (host-side count)
 };
 
 namespace {
@@ -260,6 +263,8 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
     p.dv = s->dx[0] * s->dx[1] * s->dx[2];
     p.dt_dev = &s->sc->dt;
     p.cfl = s->cfl;
+    p.dt_seq = s->dt_seq;
+    p.step_dev = &s->sc->steps;
     p.invdx0 = ix0;
     p.invdx1 = ix1;
     p.invdx2 = ix2;
@@ -273,7 +278,7 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[2], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_finalize_dt<T>(s->sc, static_cast<T>(s->cfl), 1, s->stream), "finalize launch");
+    SIM_CUDA(launch_finalize_dt<T>(s->sc, static_cast<T>(s->cfl), 1, s->stream, s->dt_seq), "finalize launch");
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[3], s->stream), "cudaEventRecord");
     }
@@ -290,6 +295,7 @@ int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
 int prepare_loaded(eulr_sim* s)
 {
     s->cur = 0;
+    s->host_steps = 0;
     SIM_CUDA(cudaMemsetAsync(s->sc, 0, sizeof(SimScalars), s->stream), "cudaMemsetAsync");
     if (is_f64(s)) {
         CBundle<double> pv = cbundle_of<double>(s->prim[0]);
@@ -398,6 +404,47 @@ int set_state_impl(eulr_sim* s, const double* const* prim, const double* const* 
 }
 
 } // namespace
+
+namespace eulr {
+
+int sim_snapshot(eulr_sim* s, double* const* dst, int nfields)
+{
+    SIM_TRY(check_sim(s));
+    if (!is_f64(s) || !s->loaded || nfields < 1 || nfields > 11) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "snapshot needs a loaded FP64 simulation and 1..11 fields");
+    }
+    size_t const bytes = static_cast<size_t>(ncell(s)) * sizeof(double);
+    for (int f = 0; f < nfields; ++f) {
+        void const* src = f < 5 ? s->prim[s->cur][f] : (f < 10 ? s->cons[s->cur][f - 5] : s->cs[s->cur]);
+        SIM_CUDA(cudaMemcpyAsync(dst[f], src, bytes, cudaMemcpyDeviceToDevice, s->stream), "snapshot copy");
+    }
+    return EULR_SUCCESS;
+}
+
+cudaStream_t sim_stream(eulr_sim* s) { return s->stream; }
+
+int sim_restore(eulr_sim* s, const double* const* src, long long step)
+{
+    SIM_TRY(check_sim(s));
+    if (!is_f64(s) || step < 0) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "restore needs an FP64 simulation and a step >= 0");
+    }
+    size_t const bytes = static_cast<size_t>(ncell(s)) * sizeof(double);
+    for (int f = 0; f < 11; ++f) {
+        void* dst = f < 5 ? s->prim[0][f] : (f < 10 ? s->cons[0][f - 5] : s->cs[0]);
+        SIM_CUDA(cudaMemcpyAsync(dst, src[f], bytes, cudaMemcpyDeviceToDevice, s->stream), "restore copy");
+    }
+    SimScalars h{};
+    h.steps = step;
+    SIM_CUDA(cudaMemcpyAsync(s->sc, &h, sizeof(h), cudaMemcpyHostToDevice, s->stream), "restore scalars");
+    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize"); // h is a stack value
+    s->cur = 0;
+    s->host_steps = step;
+    s->loaded = true;
+    return EULR_SUCCESS;
+}
+
+} // namespace eulr
 
 extern "C" {
 
@@ -530,6 +577,9 @@ int eulr_sim_destroy(eulr_sim* s)
     if (s->slab != nullptr) {
         cudaFree(s->slab);
     }
+    if (s->dt_seq != nullptr) {
+        cudaFree(s->dt_seq);
+    }
     if (s->own_stream && s->stream != nullptr) {
         cudaStreamDestroy(s->stream);
     }
@@ -591,6 +641,10 @@ int eulr_sim_advance(eulr_sim* s, int nsteps)
     if (!s->loaded) {
         return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "no state loaded");
     }
+    if (s->dt_seq != nullptr && s->host_steps + nsteps > s->dt_seq_len) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "advance past the end of the fixed dt sequence");
+    }
+    s->host_steps += nsteps;
     int left = nsteps;
     if (left > 0 && s->cur == 1) {
         SIM_TRY(enqueue_step(s, 1));
@@ -698,6 +752,35 @@ int eulr_sim_status(eulr_sim* s)
     }
     if (h.status != 0) {
         return eulr::sim_fail(EULR_ERR_NONFINITE, "a cell became non-finite or non-physical");
+    }
+    return EULR_SUCCESS;
+}
+
+int eulr_sim_set_dt_sequence(eulr_sim* s, const double* dts, long long n)
+{
+    SIM_TRY(check_sim(s));
+    if (n < 0 || (n > 0 && dts == nullptr)) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "bad dt sequence");
+    }
+    for (long long i = 0; i < n; ++i) {
+        if (!std::isfinite(dts[i]) || !(dts[i] > 0.0)) {
+            return eulr::sim_fail(EULR_ERR_INVALID_VALUE, "dt sequence entries must be finite and > 0");
+        }
+    }
+    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    if (s->dt_seq != nullptr) {
+        cudaFree(s->dt_seq);
+        s->dt_seq = nullptr;
+        s->dt_seq_len = 0;
+    }
+    if (n > 0) {
+        SIM_CUDA(cudaMalloc(&s->dt_seq, sizeof(double) * n), "cudaMalloc(dt sequence)");
+        SIM_CUDA(cudaMemcpy(s->dt_seq, dts, sizeof(double) * n, cudaMemcpyHostToDevice), "copy dt sequence");
+        s->dt_seq_len = n;
+    }
+    if (s->graph != nullptr) { // the captured launches carry the old parameters
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
     }
     return EULR_SUCCESS;
 }

@@ -71,6 +71,7 @@ _SIGNATURES = [
     ("eulr_sim_set_state_f64", _I, [_P, Bundle5, Bundle5]),
     ("eulr_sim_init_implode", _I, [_P]),
     ("eulr_sim_advance", _I, [_P, _I]),
+    ("eulr_sim_set_dt_sequence", _I, [_P, ctypes.POINTER(_D), ctypes.c_longlong]),
     ("eulr_sim_get_state_f64", _I, [_P, Bundle5, Bundle5]),
     ("eulr_sim_time", _I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_longlong)]),
     ("eulr_sim_status", _I, [_P]),
@@ -79,6 +80,17 @@ _SIGNATURES = [
     ("eulr_sim_totals", _I, [_P, ctypes.POINTER(_D)]),
     ("eulr_sim_state_bytes", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("eulr_probe_fma_rate", _I, [_I, _I, ctypes.POINTER(_D)]),
+    ("eulr_godunov_adjoint_workspace_bytes", ctypes.c_size_t, [_I, _I, _I]),
+    ("eulr_godunov_adjoint_f64", _I, [Bundle5, Bundle5, Bundle5, _I, _I, _I, _D, _D, _D, _D, _D, _P,
+                                      ctypes.c_size_t, _P]),
+    ("eulr_cons_to_prim_adjoint_f64", _I, [Bundle5, Bundle5, Bundle5, _I, _I, _I, _D, _I, _P]),
+    ("eulr_prim_to_cons_adjoint_f64", _I, [Bundle5, Bundle5, Bundle5, _I, _I, _I, _D, _I, _P]),
+    ("eulr_adjoint_create", _I, [_I, _I, _I, _D, _D, _D, _D, _D, _I, _I, _P, ctypes.POINTER(_P)]),
+    ("eulr_adjoint_destroy", _I, [_P]),
+    ("eulr_adjoint_forward", _I, [_P, Bundle5, ctypes.POINTER(_D), Bundle5]),
+    ("eulr_adjoint_dts", _I, [_P, ctypes.POINTER(_D)]),
+    ("eulr_adjoint_backward", _I, [_P, Bundle5, Bundle5]),
+    ("eulr_adjoint_timing", _I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     ("eulr_batch_create", _I, [_I, _I, _P, _D, _P, ctypes.POINTER(_P)]),
     ("eulr_batch_destroy", _I, [_P]),
     ("eulr_batch_set_prim_f64", _I, [_P, _I, Bundle5]),
@@ -271,6 +283,11 @@ class Simulation:
     def advance(self, nsteps):
         check(load().eulr_sim_advance(self._h, int(nsteps)))
 
+    def set_dt_sequence(self, dts):
+        """Fix step n's dt to dts[n] (applies from the next load)."""
+        arr = (ctypes.c_double * len(dts))(*[float(v) for v in dts])
+        check(load().eulr_sim_set_dt_sequence(self._h, arr, len(dts)))
+
     def get_state(self, prim=None, cons=None):
         """Copy the state into the given bundles (host numpy or device tensors)."""
         check(load().eulr_sim_get_state_f64(self._h, bundle(prim) if prim is not None else null_bundle(),
@@ -381,6 +398,92 @@ class Batch:
                                      ctypes.byref(kc)))
         return {"interior_cells": cells.value, "items": items.value,
                 "tile": (shape.value // 1000, shape.value % 1000), "kchunk": kc.value}
+
+
+def godunov_adjoint(prim, cons_bar, gamma, dx, dt, out=None, workspace=None, stream=None):
+    """prim_bar = (d godunov / d prim)^T cons_bar (device tensors, FP64)."""
+    torch = _torch()
+    n0, n1, n2 = dims(prim)
+    need = load().eulr_godunov_adjoint_workspace_bytes(n0, n1, n2)
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=prim.device)
+    prim_bar = out if out is not None else torch.empty_like(prim)
+    check(load().eulr_godunov_adjoint_f64(bundle(prim), bundle(cons_bar), bundle(prim_bar), n0, n1, n2,
+                                          float(gamma), float(dx[0]), float(dx[1]), float(dx[2]), float(dt),
+                                          ctypes.c_void_p(workspace.data_ptr()), workspace.numel(),
+                                          _stream(stream)))
+    return prim_bar
+
+
+def cons_to_prim_adjoint(prim, prim_bar, gamma, out=None, accumulate=False, stream=None):
+    """cons_bar (+)= cons_to_prim'(state with primitive variables prim)^T prim_bar."""
+    cons_bar = out if out is not None else _torch().empty_like(prim)
+    check(load().eulr_cons_to_prim_adjoint_f64(bundle(prim), bundle(prim_bar), bundle(cons_bar), *dims(prim),
+                                               float(gamma), int(bool(accumulate)), _stream(stream)))
+    return cons_bar
+
+
+def prim_to_cons_adjoint(prim, cons_bar, gamma, out=None, accumulate=False, stream=None):
+    """prim_bar (+)= prim_to_cons'(prim)^T cons_bar."""
+    prim_bar = out if out is not None else _torch().empty_like(prim)
+    check(load().eulr_prim_to_cons_adjoint_f64(bundle(prim), bundle(cons_bar), bundle(prim_bar), *dims(prim),
+                                               float(gamma), int(bool(accumulate)), _stream(stream)))
+    return prim_bar
+
+
+class Adjoint:
+    """Checkpointed time-loop adjoint (eulr_adjoint_*): forward from prim0,
+    backward from dJ/d(final prim) to dJ/d prim0."""
+
+    def __init__(self, n0, n1, n2, nsteps, gamma=1.4, dx=None, cfl=0.4, checkpoint_every=20, stream=None):
+        self.shape = (n0, n1, n2)
+        if dx is None:
+            dx = (1.0 / (n0 - 2), 1.0 / (n1 - 2), 1.0 / (n2 - 2))
+        self.dx = tuple(float(v) for v in dx)
+        self.gamma = float(gamma)
+        self.nsteps = int(nsteps)
+        h = ctypes.c_void_p()
+        s = ctypes.c_void_p(stream.cuda_stream) if stream is not None else ctypes.c_void_p(None)
+        check(load().eulr_adjoint_create(n0, n1, n2, self.gamma, *self.dx, float(cfl), self.nsteps,
+                                         int(checkpoint_every), s, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().eulr_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, prim0, dts=None, out=None):
+        """Runs the forward pass; dts fixes every step's dt (else CFL steps).
+        Writes the final prim into out (a bundle) when given."""
+        arr = None
+        if dts is not None:
+            if len(dts) != self.nsteps:
+                raise ValueError(f"need {self.nsteps} step lengths, got {len(dts)}")
+            arr = (ctypes.c_double * self.nsteps)(*[float(v) for v in dts])
+        check(load().eulr_adjoint_forward(self._h, bundle(prim0), arr,
+                                          bundle(out) if out is not None else null_bundle()))
+        return out
+
+    def dts(self):
+        arr = (ctypes.c_double * max(self.nsteps, 1))()
+        check(load().eulr_adjoint_dts(self._h, arr))
+        return [arr[i] for i in range(self.nsteps)]
+
+    def backward(self, prim_final_bar, out):
+        check(load().eulr_adjoint_backward(self._h, bundle(prim_final_bar), bundle(out)))
+        return out
+
+    def timing(self):
+        f, r, v = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(load().eulr_adjoint_timing(self._h, ctypes.byref(f), ctypes.byref(r), ctypes.byref(v)))
+        return {"forward_ms": f.value, "recompute_ms": r.value, "reverse_ms": v.value}
 
 
 def fma_rate(kind: str = "f64", iters: int = 20000) -> float:

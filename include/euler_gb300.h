@@ -230,6 +230,13 @@ int eulr_sim_init_implode(eulr_sim* sim);
 /* Advance nsteps steps (asynchronous; replays a CUDA graph). */
 int eulr_sim_advance(eulr_sim* sim, int nsteps);
 
+/* Fix the time step: from the next load on, step n (counted from the
+ * loaded state) uses dt = dts[n] (the step length itself; no CFL factor)
+ * instead of the CFL time step; advancing past n steps is an error.  n = 0
+ * returns to CFL time steps.  dts is host memory, copied.  Used to hold dt
+ * at a forward sequence (adjoint checks, finite differences). */
+int eulr_sim_set_dt_sequence(eulr_sim* sim, const double* dts, long long n);
+
 /* Copy the current state out (host or device destination); waits for the
  * stream.  Either bundle pointer set may be all-NULL to skip it. */
 int eulr_sim_get_state_f64(eulr_sim* sim, eulr_prim_f64 prim, eulr_cons_f64 cons);
@@ -304,6 +311,69 @@ int eulr_batch_status(eulr_batch* batch);
 /* Interior cells of all grids, work items per step, tile shape (TX*1000+TY)
  * and chunk length in use (any may be NULL). */
 int eulr_batch_info(eulr_batch* batch, long long* interior_cells, int* nitems, int* tile_shape, int* kchunk);
+
+/* ---------------------------------------------------------------- adjoint
+ * Reverse mode of the time step (no counterpart in the reference, which has
+ * no derivatives).  What is differentiated is the reference's step with dt
+ * held fixed: godunov (godunov.hpp:15-92, HLLC flux hllc.hpp:50-105) then
+ * cons_to_prim (cons_to_prim.hpp:7-33), and prim_to_cons
+ * (prim_to_cons.hpp:7-33) before the first step.  The HLLC flux is piecewise
+ * smooth; at exact ties (equal arguments of its min/max, ustar == 0 in the
+ * subsonic case) the derivative is the mean of the two one-sided ones, as a
+ * central difference measures.  All pointers are device memory. */
+
+/* Bytes of device workspace eulr_godunov_adjoint_f64 needs for a grid
+ * (40 FP64 fields of n0*n1*n2 values, each padded to 256 bytes); 0 when the
+ * extents are invalid. */
+size_t eulr_godunov_adjoint_workspace_bytes(int n0, int n1, int n2);
+
+/* Transpose of godunov with respect to prim: given cons_bar, the gradient of
+ * a functional with respect to the cons that godunov(prim, cons, dt)
+ * produces, writes prim_bar = (d godunov / d prim)^T cons_bar.  (With respect
+ * to the incoming cons the update is the identity.)  The face solves are
+ * recomputed from prim; each cell sums its six face terms without atomics.
+ * workspace: device memory of eulr_godunov_adjoint_workspace_bytes bytes,
+ * 256-byte aligned.  prim_bar must not overlap prim or cons_bar. */
+int eulr_godunov_adjoint_f64(eulr_prim_cf64 prim, eulr_cons_cf64 cons_bar, eulr_prim_f64 prim_bar, int n0, int n1,
+                             int n2, double gamma, double dx0, double dx1, double dx2, double dt, void* workspace,
+                             size_t workspace_bytes, eulr_stream_t stream);
+
+/* Transpose of cons_to_prim at the state whose primitive variables are prim:
+ * cons_bar = cons_to_prim'^T prim_bar, or cons_bar += ... when accumulate is
+ * nonzero.  Pointwise; cons_bar must not overlap prim or prim_bar. */
+int eulr_cons_to_prim_adjoint_f64(eulr_prim_cf64 prim, eulr_prim_cf64 prim_bar, eulr_cons_f64 cons_bar, int n0,
+                                  int n1, int n2, double gamma, int accumulate, eulr_stream_t stream);
+
+/* Transpose of prim_to_cons at prim: prim_bar (+)= prim_to_cons'^T cons_bar. */
+int eulr_prim_to_cons_adjoint_f64(eulr_prim_cf64 prim, eulr_cons_cf64 cons_bar, eulr_prim_f64 prim_bar, int n0,
+                                  int n1, int n2, double gamma, int accumulate, eulr_stream_t stream);
+
+/* Checkpointed time-loop adjoint.  eulr_adjoint_forward runs the FP64 fused
+ * simulation from prim0 for nsteps steps, keeping the state every
+ * checkpoint_every steps; eulr_adjoint_backward maps the gradient of a
+ * functional with respect to the final prim to its gradient with respect to
+ * prim0, recomputing each segment's states from its checkpoint and then
+ * applying the reverse steps (prep, face and gather kernels per step). */
+typedef struct eulr_adjoint eulr_adjoint;
+
+int eulr_adjoint_create(int n0, int n1, int n2, double gamma, double dx0, double dx1, double dx2, double cfl,
+                        int nsteps, int checkpoint_every, eulr_stream_t stream, eulr_adjoint** out);
+int eulr_adjoint_destroy(eulr_adjoint* adj);
+
+/* Forward pass from prim0 (host or device).  dts: host array of nsteps step
+ * lengths to hold dt fixed at, or NULL for CFL time steps (recorded; read
+ * them with eulr_adjoint_dts).  prim_final (host or device; all-NULL skips
+ * it) receives the final prim.  Synchronous. */
+int eulr_adjoint_forward(eulr_adjoint* adj, eulr_prim_cf64 prim0, const double* dts, eulr_prim_f64 prim_final);
+/* The nsteps step lengths of the last forward pass (host array). */
+int eulr_adjoint_dts(eulr_adjoint* adj, double* dts);
+/* Reverse pass: prim_final_bar = dJ/d(final prim) (host or device) ->
+ * prim0_bar = dJ/d prim0 (host or device).  Needs a forward pass first.
+ * Synchronous. */
+int eulr_adjoint_backward(eulr_adjoint* adj, eulr_prim_cf64 prim_final_bar, eulr_prim_f64 prim0_bar);
+/* Device time of the last passes in ms: the forward pass, the recompute of
+ * the checkpointed segments, and the reverse steps (any may be NULL). */
+int eulr_adjoint_timing(eulr_adjoint* adj, double* forward_ms, double* recompute_ms, double* reverse_ms);
 
 /* ------------------------------------------------------------ measurement */
 

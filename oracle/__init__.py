@@ -30,6 +30,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libeuler_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libeuler_ref.so")
+REF_TLM_SO = os.path.join(HERE, "_ref", "libeuler_ref_tlm.so")
 REFERENCE_DIR = "/root/reference"
 
 _DT = {"f64": (np.float64, ctypes.c_double), "f32": (np.float32, ctypes.c_float)}
@@ -47,6 +48,10 @@ def build(ref: bool | None = None) -> None:
 
 def have_ref() -> bool:
     return os.path.exists(REF_SO)
+
+
+def have_ref_tlm() -> bool:
+    return os.path.exists(REF_TLM_SO)
 
 
 def _lib(impl: str) -> tuple[ctypes.CDLL, str]:
@@ -153,6 +158,69 @@ def simulate(prim: np.ndarray, cons: np.ndarray, gamma: float, dx, cfl: float, n
         int(nsteps), ctypes.byref(t),
     )
     return t.value
+
+
+# ---------------------------------------------------- tangent-linear model
+# Forward-mode derivative of the step with dt fixed (oracle/euler_tlm.c, and
+# with impl="ref" the reference's own operators instantiated on dual numbers,
+# oracle/ref_tlm.cpp).  Each function takes and returns (value, tangent)
+# bundles.
+
+def _tlm_fn(impl: str, name: str):
+    if impl == "port":
+        lib, _ = _lib("port")
+        return getattr(lib, f"oracle_tlm_{name}_f64")
+    if impl == "ref":
+        if "ref_tlm" not in _libs:
+            if not os.path.exists(REF_TLM_SO):
+                raise FileNotFoundError(f"oracle library {REF_TLM_SO} is not built (run oracle.build())")
+            _libs["ref_tlm"] = ctypes.CDLL(REF_TLM_SO)
+        return getattr(_libs["ref_tlm"], f"ref_tlm_{name}_f64")
+    raise ValueError(f"unknown oracle implementation {impl!r}")
+
+
+def _f64(*arrays):
+    for a in arrays:
+        if a.dtype != np.float64:
+            raise TypeError("the tangent-linear model is FP64")
+
+
+def tlm_prim_to_cons(prim, dprim, gamma, impl="port"):
+    _f64(prim, dprim)
+    cons, dcons = np.zeros_like(prim), np.zeros_like(prim)
+    _tlm_fn(impl, "prim_to_cons")(_ptrs(prim), _ptrs(dprim), _ptrs(cons), _ptrs(dcons), *_dims(prim),
+                                  ctypes.c_double(gamma))
+    return cons, dcons
+
+
+def tlm_cons_to_prim(cons, dcons, gamma, impl="port"):
+    _f64(cons, dcons)
+    prim, dprim = np.zeros_like(cons), np.zeros_like(cons)
+    _tlm_fn(impl, "cons_to_prim")(_ptrs(cons), _ptrs(dcons), _ptrs(prim), _ptrs(dprim), *_dims(cons),
+                                  ctypes.c_double(gamma))
+    return prim, dprim
+
+
+def tlm_godunov(prim, dprim, cons, dcons, gamma, dx, dt, impl="port"):
+    """Updated copies of (cons, dcons) after godunov(prim, cons, dt)."""
+    _f64(prim, dprim, cons, dcons)
+    out, dout = cons.copy(), dcons.copy()
+    D = ctypes.c_double
+    _tlm_fn(impl, "godunov")(_ptrs(prim), _ptrs(dprim), _ptrs(out), _ptrs(dout), *_dims(prim), D(gamma), D(dx[0]),
+                             D(dx[1]), D(dx[2]), D(dt))
+    return out, dout
+
+
+def tlm_simulate(prim0, dprim0, gamma, dx, dts):
+    """(prim, dprim) after len(dts) steps of fixed dt from (prim0, dprim0) (port)."""
+    _f64(prim0, dprim0)
+    prim, dprim = prim0.copy(), dprim0.copy()
+    cons, dcons = np.zeros_like(prim), np.zeros_like(prim)
+    D = ctypes.c_double
+    arr = (ctypes.c_double * max(len(dts), 1))(*[float(v) for v in dts])
+    _tlm_fn("port", "simulate")(_ptrs(prim), _ptrs(dprim), _ptrs(cons), _ptrs(dcons), *_dims(prim), D(gamma),
+                                D(dx[0]), D(dx[1]), D(dx[2]), arr, len(dts))
+    return prim, dprim
 
 
 def random_prim(n0, n1, n2, seed=0, dtype=np.float64) -> np.ndarray:
