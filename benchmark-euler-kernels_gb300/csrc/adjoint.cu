@@ -19,11 +19,13 @@
 //              step never updates).
 //   adj_face   per cell, its three upper faces: the HLLC solve recomputed
 //              from prim_n (nothing of the forward solve is stored), then
-//              its transpose applied to g = ds (w_R - w_L).  Each face
-//              stores its left and right halves (5 values each) apart.
-//   adj_gather per cell: the sum of its six face halves -- every cell reads
-//              only its own halves, so there are no atomics -- then the
-//              cons_to_prim or prim_to_cons transpose.
+//              its transpose applied to g = ds (w_R - w_L).  The cell keeps
+//              the sum of the three left halves (its own) and stores the
+//              right half of each face (the neighbour's) apart.
+//   adj_gather per cell: its own sum plus the right halves its three lower
+//              neighbours stored -- every cell reads only halves meant for
+//              it, so there are no atomics -- then the cons_to_prim or
+//              prim_to_cons transpose.
 //
 // Ties.  The HLLC flux is piecewise smooth: it takes min/max of wave-speed
 // estimates and branches on the sign of ustar.  At an exact tie (equal
@@ -90,6 +92,7 @@ __global__ void __launch_bounds__(kThreads) adj_prep_kernel(AdjParams p)
         p.w.derived[2][c] = -0.5 * cs * inv_d;
         p.w.derived[3][c] = pr * p.inv_gm1 + d * ke;
         p.w.derived[4][c] = ke;
+        p.w.derived[5][c] = inv_d;
         int i, j, k;
         decode(p.g, c, i, j, k);
         bool const in = interior(p.g, i, j, k);
@@ -116,16 +119,9 @@ __device__ __forceinline__ FaceSide load_side(AdjParams const& p, long long c, i
     return s;
 }
 
-__device__ __forceinline__ void store_half(AdjParams const& p, int a, int side, long long c, FaceBar const& b)
-{
-    double* const* f = p.w.face + (a * 2 + side) * 5;
-    f[0][c] = b.r;
-    f[1][c] = b.p;
-    f[2 + a][c] = b.un;
-    f[2 + (a + 1) % 3][c] = b.t1;
-    f[2 + (a + 2) % 3][c] = b.t2;
-}
-
+// The face halves a cell stores: its own sum over the left halves of its three
+// upper faces (index f), and the right half of each upper face (5 + a*5 + f),
+// which belongs to the neighbour c + e_a.
 __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
 {
     long long const n = p.g.ncell();
@@ -135,6 +131,7 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
         int idx[3];
         decode(p.g, c, idx[0], idx[1], idx[2]);
         int const ext[3] = {p.g.n0, p.g.n1, p.g.n2};
+        double self[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll 1
         for (int a = 0; a < 3; ++a) {
             int const b = (a + 1) % 3, e = (a + 2) % 3;
@@ -146,17 +143,36 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
             zero(bR);
             if (active) {
                 long long const cr = c + stride[a];
-                double g[5];
+                double dw[5];
+                bool any = false;
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    g[f] = p.ds[a] * (p.w.weight[f][cr] - p.w.weight[f][c]);
+                    dw[f] = p.w.weight[f][cr] - p.w.weight[f][c];
+                    any = any || dw[f] != 0.0;
                 }
-                FaceSide const L = load_side(p, c, a);
-                FaceSide const R = load_side(p, cr, a);
-                hllc_bar(L, R, g[0], g[1], g[2 + a], g[2 + b], g[2 + e], p.inv_gm1, bL, bR);
+                // a face outside the cotangent's support contributes nothing (early reverse
+                // steps: the support is the functional's region grown by one cell per step)
+                if (any) {
+                    FaceSide const L = load_side(p, c, a);
+                    FaceSide const R = load_side(p, cr, a);
+                    hllc_bar(L, R, dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], p.ds[a], p.inv_gm1, bL, bR);
+                }
             }
-            store_half(p, a, 0, c, bL);
-            store_half(p, a, 1, c, bR);
+            self[0] += bL.r;
+            self[1] += bL.p;
+            self[2 + a] += bL.un;
+            self[2 + b] += bL.t1;
+            self[2 + e] += bL.t2;
+            double* const* fr = p.w.face + 5 + a * 5;
+            fr[0][c] = bR.r;
+            fr[1][c] = bR.p;
+            fr[2 + a][c] = bR.un;
+            fr[2 + b][c] = bR.t1;
+            fr[2 + e][c] = bR.t2;
+        }
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            p.w.face[f][c] = self[f];
         }
     }
 }
@@ -172,22 +188,21 @@ __global__ void __launch_bounds__(kThreads) adj_gather_kernel(AdjParams p)
         double pb[5];
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
-            double s = 0.0;
+            double s = p.w.face[f][c]; // faces where this cell is the left side
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                s += p.w.face[(a * 2 + 0) * 5 + f][c]; // faces where this cell is the left side
                 if (idx[a] >= 1) {
-                    s += p.w.face[(a * 2 + 1) * 5 + f][c - stride[a]]; // ... and the right side
+                    s += p.w.face[5 + a * 5 + f][c - stride[a]]; // ... and the right side
                 }
             }
             pb[f] = s;
         }
         double const d = p.prim.f[0][c];
         double const u0 = p.prim.f[2][c], u1 = p.prim.f[3][c], u2 = p.prim.f[4][c];
-        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        double const ke = p.w.derived[4][c];
         if (p.mode == kAdjStep) {
             // cons_to_prim: p = (gamma-1)(e - |m|^2/(2d)), u = m/d
-            double const inv_d = __drcp_rn(d);
+            double const inv_d = p.w.derived[5][c];
             double const gp = pb[1] * p.gm1;
             double const c0 = p.cbar.f[0][c], c1 = p.cbar.f[1][c];
             double const c2 = p.cbar.f[2][c], c3 = p.cbar.f[3][c], c4 = p.cbar.f[4][c];
@@ -281,10 +296,10 @@ AdjWork adjoint_workspace(void* base, long long ncell)
     AdjWork w{};
     size_t const field = pad_field(ncell);
     char* p = static_cast<char*>(base);
-    for (int f = 0; f < 30; ++f, p += field) {
+    for (int f = 0; f < 20; ++f, p += field) {
         w.face[f] = reinterpret_cast<double*>(p);
     }
-    for (int f = 0; f < 5; ++f, p += field) {
+    for (int f = 0; f < 6; ++f, p += field) {
         w.derived[f] = reinterpret_cast<double*>(p);
     }
     for (int f = 0; f < 5; ++f, p += field) {

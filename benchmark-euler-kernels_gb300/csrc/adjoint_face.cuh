@@ -73,11 +73,24 @@ EULR_ADJ_FN double star_branch_bar(FaceSide const& q, double S, double a, double
     return gY + ga;
 }
 
-// Transposed HLLC flux of one face (hllc.hpp:50-105): given the cotangent of
-// the face flux in the face frame (gd, ge, gn, gt1, gt2), adds the cotangents
-// of both sides' primitive states to bL and bR.
-EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double gd, double ge, double gn, double gt1,
-                                         double gt2, double inv_gm1, FaceBar& bL, FaceBar& bR)
+// star_branch_bar at ustar == 0 (iS = 1/S_Q): returns the branch's d/d ustar;
+// its d/d pstar is gn and it adds nothing to bq or d/d S_Q.
+EULR_ADJ_FN double tie_branch_bar(FaceSide const& q, double a, double iS, double pstar, double gd, double ge,
+                                  double gt1, double gt2)
+{
+    double const r = a * iS;
+    double const d_o = r * q.r;
+    double const eo = r * q.e - (q.p * q.un) * iS;
+    double const gm = gd + gt1 * q.t1 + gt2 * q.t2;
+    return ge * (eo + pstar) + gm * d_o;
+}
+
+// Transposed HLLC flux of one face (hllc.hpp:50-105).  The cotangent of the
+// face flux is ds * (dd, de, dn, dt1, dt2) in the face frame (mass, energy,
+// normal and tangential momentum); adds the cotangents of both sides'
+// primitive states to bL and bR.
+EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, double de, double dn, double dt1,
+                          double dt2, double ds, double inv_gm1, FaceBar& bL, FaceBar& bR)
 {
     // S_L = min(un_L, un_R) - max(c_L, c_R), S_R = max(un_L, un_R) + max(c_L, c_R)
     bool const u_lt = L.un < R.un;
@@ -97,6 +110,9 @@ EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double gd, doubl
     double const den = rcL - rcR; // rcL <= 0 <= rcR: den < 0, so ustar > 0 exactly when num < 0
     bool const left = num < 0.0;
     bool const tie = num == 0.0;
+    // at a tie each of the two branches takes half of the cotangent
+    double const sc = tie ? 0.5 * ds : ds;
+    double const gd = sc * dd, ge = sc * de, gn = sc * dn, gt1 = sc * dt1, gt2 = sc * dt2;
 
     if (SL > 0.0 || SR < 0.0) {
         // S_L * S_R > 0: the flux is the upwind side's physical flux (ustar > 0 picks L)
@@ -113,27 +129,37 @@ EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double gd, doubl
         return;
     }
 
-    // One reciprocal gives 1/den and 1/(S - ustar): with Z = S den - num,
-    // S - ustar = Z/den, so 1/den = Z R and 1/(S - ustar) = den^2 R for R = 1/(den Z).
-    double const S0 = left ? SL : SR;
-    double const Z = S0 * den - num;
-    double const Rr = adj_rcp(den * Z);
-    double const inv_den = Z * Rr;
-    double const iY0 = (den * den) * Rr;
-    double const ustar = num * inv_den;
-    double const pstar = 0.5 * (L.p + R.p + rcL * (ustar - L.un) + rcR * (ustar - R.un));
-
+    double inv_den, ustar, pstar;
     double gus = 0.0, gps = 0.0, gSL = 0.0, gSR = 0.0;
-    double const w = tie ? 0.5 : 1.0;
-    double const hd = w * gd, he = w * ge, hn = w * gn, h1 = w * gt1, h2 = w * gt2;
-    if (left) {
-        gSL += star_branch_bar(L, SL, aL, iY0, ustar, pstar, hd, he, hn, h1, h2, inv_gm1, gus, gps, bL);
+    if (tie) {
+        // ustar == 0: the mean of the two star branches.  With ustar = 0 the
+        // mass flux m = d_o ustar vanishes, and so does every cotangent that
+        // carries a factor ustar: each branch adds only its mass and energy
+        // terms to d/d ustar and gn to d/d pstar (star_branch_bar with ustar = 0).
+        // One reciprocal gives 1/den, 1/S_L and 1/S_R.
+        double const P = SL * SR;
+        double const Rr = adj_rcp(den * P);
+        inv_den = P * Rr;
+        ustar = 0.0;
+        pstar = 0.5 * (L.p + R.p - rcL * L.un - rcR * R.un);
+        gus = tie_branch_bar(L, aL, (den * SR) * Rr, pstar, gd, ge, gt1, gt2) +
+              tie_branch_bar(R, aR, (den * SL) * Rr, pstar, gd, ge, gt1, gt2);
+        gps = 2.0 * gn;
     } else {
-        gSR += star_branch_bar(R, SR, aR, iY0, ustar, pstar, hd, he, hn, h1, h2, inv_gm1, gus, gps, bR);
-    }
-    if (tie) { // the forward took R; add the mean with the L branch
-        double const iY1 = adj_rcp(SL - ustar);
-        gSL += star_branch_bar(L, SL, aL, iY1, ustar, pstar, hd, he, hn, h1, h2, inv_gm1, gus, gps, bL);
+        // One reciprocal gives 1/den and 1/(S - ustar): with Z = S den - num,
+        // S - ustar = Z/den, so 1/den = Z R and 1/(S - ustar) = den^2 R for R = 1/(den Z).
+        double const S0 = left ? SL : SR;
+        double const Z = S0 * den - num;
+        double const Rr = adj_rcp(den * Z);
+        inv_den = Z * Rr;
+        double const iY0 = (den * den) * Rr;
+        ustar = num * inv_den;
+        pstar = 0.5 * (L.p + R.p + rcL * (ustar - L.un) + rcR * (ustar - R.un));
+        if (left) {
+            gSL = star_branch_bar(L, SL, aL, iY0, ustar, pstar, gd, ge, gn, gt1, gt2, inv_gm1, gus, gps, bL);
+        } else {
+            gSR = star_branch_bar(R, SR, aR, iY0, ustar, pstar, gd, ge, gn, gt1, gt2, inv_gm1, gus, gps, bR);
+        }
     }
 
     // pstar = (p_L + p_R + rc_L (ustar - un_L) + rc_R (ustar - un_R)) / 2

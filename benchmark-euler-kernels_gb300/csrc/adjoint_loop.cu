@@ -7,13 +7,15 @@
 // Each is recomputed from its checkpoint with the recorded dt sequence --
 // bit-identical to the forward pass -- keeping prim_n of every step in the
 // segment, and then the reverse steps (adjoint.cu) run from its last step
-// down to its first.  Memory: ceil(nsteps/k) checkpoints of 11 fields plus
-// k+1 primitive states, instead of nsteps states.
+// down to its first.  A segment of k steps needs prim_n for its k steps, so
+// it recomputes k-1 steps (none when k = 1); the final state is kept from
+// the forward pass.  Memory: ceil(nsteps/k) checkpoints of 11 fields plus k
+// primitive states, instead of nsteps states.
 //
 // Device memory (one allocation, fields of n0*n1*n2 doubles padded to 256 B):
 //   checkpoints   nckpt x 11
-//   segment prims (k + 1) x 5
-//   cbar 5, prim0_bar 5, final prim_bar 5
+//   segment prims k x 5
+//   cbar 5, prim0_bar 5, final prim_bar 5, final prim 5
 //   reverse-step workspace kAdjWorkFields
 #include "euler_gb300.h"
 #include "kernels.h"
@@ -44,12 +46,13 @@ struct eulr_adjoint {
     double* at(size_t index) const { return reinterpret_cast<double*>(static_cast<char*>(slab) + field * index); }
     double* ckpt(int c, int f) const { return at(static_cast<size_t>(c) * 11 + f); }
     double* seg(int n, int f) const { return at(static_cast<size_t>(nckpt) * 11 + static_cast<size_t>(n) * 5 + f); }
-    size_t tail() const { return static_cast<size_t>(nckpt) * 11 + static_cast<size_t>(every + 1) * 5; }
+    size_t tail() const { return static_cast<size_t>(nckpt) * 11 + static_cast<size_t>(every) * 5; }
     double* cbar(int f) const { return at(tail() + f); }
     double* pbar0(int f) const { return at(tail() + 5 + f); }
     double* pbarT(int f) const { return at(tail() + 10 + f); }
-    void* work() const { return at(tail() + 15); }
-    size_t nfields() const { return tail() + 15 + kAdjWorkFields; }
+    double* primN(int f) const { return at(tail() + 15 + f); }
+    void* work() const { return at(tail() + 20); }
+    size_t nfields() const { return tail() + 20 + kAdjWorkFields; }
 };
 
 namespace {
@@ -262,6 +265,11 @@ int eulr_adjoint_forward(eulr_adjoint* a, eulr_prim_cf64 prim0, const double* dt
         }
     }
     ADJ_CUDA(cudaEventRecord(span.b, a->stream), "cudaEventRecord");
+    double* fin[5];
+    for (int f = 0; f < 5; ++f) {
+        fin[f] = a->primN(f);
+    }
+    ADJ_TRY(eulr::sim_snapshot(a->sim, fin, 5));
     ADJ_TRY(eulr_sim_status(a->sim));
     ADJ_TRY(eulr_sim_get_state_f64(a->sim, prim_final, eulr_cons_f64{nullptr, nullptr, nullptr, nullptr, nullptr}));
     a->fwd_ms = span.ms();
@@ -327,14 +335,13 @@ int eulr_adjoint_backward(eulr_adjoint* a, eulr_prim_cf64 prim_final_bar, eulr_p
             src[f] = a->ckpt(c, f);
         }
         ADJ_TRY(eulr::sim_restore(a->sim, src, s0));
-        int const last = (c == a->nckpt - 1) ? s1 : s1 - 1; // the final state is needed once
-        for (int n = s0; n <= last; ++n) {
+        for (int n = s0; n < s1; ++n) {
             double* dst[5];
             for (int f = 0; f < 5; ++f) {
                 dst[f] = a->seg(n - s0, f);
             }
             ADJ_TRY(eulr::sim_snapshot(a->sim, dst, 5));
-            if (n < s1) {
+            if (n + 1 < s1) {
                 ADJ_TRY(eulr_sim_advance(a->sim, 1));
             }
         }
@@ -343,7 +350,7 @@ int eulr_adjoint_backward(eulr_adjoint* a, eulr_prim_cf64 prim_final_bar, eulr_p
         if (c == a->nckpt - 1) { // dJ/dcons_N = cons_to_prim'(prim_N)^T dJ/dprim_N
             double* pN[5];
             for (int f = 0; f < 5; ++f) {
-                pN[f] = a->seg(s1 - s0, f);
+                pN[f] = a->primN(f);
             }
             ADJ_CUDA(launch_cons_to_prim_adjoint(cb(pN), cb(pT), bb(cbar), 0, a->ncell, a->gamma, a->sms, a->stream),
                      "cons_to_prim adjoint");

@@ -70,14 +70,14 @@ extern "C" void host_godunov_adjoint(const double* const* prim, const double* co
                 continue;
             }
             long long const cr = c + stride[a];
-            double g[5];
+            double dw[5];
             for (int f = 0; f < 5; ++f) {
-                g[f] = ds[a] * (w[cr * 5 + f] - w[c * 5 + f]);
+                dw[f] = w[cr * 5 + f] - w[c * 5 + f];
             }
             FaceBar bL, bR;
             zero(bL);
             zero(bR);
-            hllc_bar(side(c, a), side(cr, a), g[0], g[1], g[2 + a], g[2 + b], g[2 + e], inv_gm1, bL, bR);
+            hllc_bar(side(c, a), side(cr, a), dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], ds[a], inv_gm1, bL, bR);
             double const lv[5] = {bL.r, bL.p, bL.un, bL.t1, bL.t2};
             double const rv[5] = {bR.r, bR.p, bR.un, bR.t1, bR.t2};
             int const map[5] = {0, 1, 2 + a, 2 + b, 2 + e};

@@ -185,3 +185,100 @@ def test_adjoint_argument_errors(cuda, euler):
     prim = torch.ones_like(g)
     with pytest.raises(euler.EulerError):  # output aliases the input
         euler.godunov_adjoint(prim, g, GAMMA, (0.1,) * 3, 1e-3, out=prim)
+
+
+def _c5_case(torch, euler, O, nx, nsteps, every, seed=0):
+    n = nx + 2
+    prim0 = implode_noise(O, nx, seed=seed)
+    w = box_weight(nx)
+    adj = euler.Adjoint(n, n, n, nsteps, gamma=GAMMA, checkpoint_every=every)
+    out = torch.empty((5, n, n, n), dtype=torch.float64, device="cuda")
+    adj.forward(torch.from_numpy(prim0).cuda(), out=out)
+    dts = adj.dts()
+    gT = torch.zeros_like(out)
+    gT[0] = torch.from_numpy(w).cuda()
+    g0 = torch.empty_like(out)
+    adj.backward(gT, g0)
+    return prim0, w, dts, g0.cpu().numpy(), adj
+
+
+def _central_differences(torch, euler, prim0, w, dts, grad, ndirs, eps=1e-6, seed=2024):
+    n2, n1, n0 = prim0.shape[1:]
+    nx = n0 - 2
+    rng = np.random.default_rng(seed)
+    wt = torch.from_numpy(w).cuda()
+    rows = []
+    with euler.Simulation(n0, n1, n2, GAMMA, (1.0 / nx,) * 3) as sim:
+        sim.set_dt_sequence(dts)
+        p = torch.empty((5, n2, n1, n0), dtype=torch.float64, device="cuda")
+        for _ in range(ndirs):
+            v = np.zeros_like(prim0)
+            v[0] = rng.normal(size=prim0.shape[1:])
+            v[1] = rng.normal(size=prim0.shape[1:])
+            vals = []
+            for s in (1.0, -1.0):
+                sim.set_prim(torch.from_numpy(prim0 + s * eps * v).cuda())
+                sim.advance(len(dts))
+                sim.get_state(prim=p)
+                vals.append(float((p[0] * wt).sum()))
+            rows.append((float(np.sum(grad * v)), (vals[0] - vals[1]) / (2 * eps), v))
+    return rows
+
+
+def test_differentiation_workload_reduced(cuda, euler, oracle_lib):
+    """The differentiation workload on a 64^3 grid for 100 steps: gradient
+    against the tangent-linear model (tight) and central differences (eps =
+    1e-6).  Central differences of this solver carry errors of ~1e-5 of the
+    directional derivatives' size: the flux has kinks at the initial state
+    (ustar == 0 on every face of the quiet gas) and near it, and the host
+    tangent-linear model, which shares no code with the GPU, shows the same
+    spread against them; the bound below is that measured spread with margin."""
+    torch, O = cuda, oracle_lib
+    nx, nsteps = 64, 100
+    prim0, w, dts, grad, _ = _c5_case(torch, euler, O, nx, nsteps, 20)
+    rng = np.random.default_rng(9)
+    for _ in range(2):
+        v = np.zeros_like(prim0)
+        v[0] = rng.normal(size=prim0.shape[1:])
+        v[1] = rng.normal(size=prim0.shape[1:])
+        _, dT = O.tlm_simulate(prim0, v, GAMMA, (1.0 / nx,) * 3, dts)
+        ref = float(np.sum(w * dT[0]))
+        # the GPU forward pass and the oracle's agree to ~1e-12 here, not bit
+        # for bit, and the derivative of a piecewise-smooth solver moves with
+        # its linearisation point wherever a face sits that close to a kink
+        assert abs(float(np.sum(grad * v)) - ref) <= 1e-7 * abs(ref)
+    rows = _central_differences(torch, euler, prim0, w, dts, grad, 4)
+    rms = float(np.sqrt(np.mean([a * a for a, _, _ in rows])))
+    for a, fd, _ in rows:
+        assert abs(fd - a) <= 2e-4 * rms, (a, fd)
+
+
+@pytest.mark.skipif(not __import__("os").environ.get("EULER_FULL_DIFFERENTIATION"),
+                    reason="full-size differentiation check (minutes of host time); set EULER_FULL_DIFFERENTIATION=1")
+def test_differentiation_workload_full(cuda, euler, oracle_lib):
+    """128^3, 400 steps, checkpoints every 20: the gradient against the host
+    tangent-linear model along one direction, and 16 central differences;
+    prints one JSON line with the figures."""
+    import json
+    import time
+
+    torch, O = cuda, oracle_lib
+    nx, nsteps = 128, 400
+    t0 = time.perf_counter()
+    prim0, w, dts, grad, adj = _c5_case(torch, euler, O, nx, nsteps, 20)
+    t_adj = time.perf_counter() - t0
+    rows = _central_differences(torch, euler, prim0, w, dts, grad, 16)
+    a, fd, v = rows[0]
+    t0 = time.perf_counter()
+    _, dT = O.tlm_simulate(prim0, v, GAMMA, (1.0 / nx,) * 3, dts)
+    t_tlm = time.perf_counter() - t0
+    tlm = float(np.sum(w * dT[0]))
+    rms = float(np.sqrt(np.mean([r[0] ** 2 for r in rows])))
+    rec = {"differentiation_full": {
+        "grid": f"{nx}^3", "steps": nsteps, "checkpoint_every": 20, "adjoint_wall_s": t_adj,
+        "tlm_wall_s": t_tlm, "tlm": tlm, "adjoint": a, "adjoint_vs_tlm_rel": abs(a - tlm) / abs(tlm),
+        "fd_vs_tlm_rel": abs(fd - tlm) / abs(tlm),
+        "fd_rel_errs": [abs(f - g) / abs(g) for g, f, _ in rows],
+        "fd_max_err_over_rms": max(abs(f - g) for g, f, _ in rows) / rms}}
+    print(json.dumps(rec))
+    assert abs(a - tlm) <= 1e-6 * abs(tlm)
