@@ -56,6 +56,12 @@ CFL = 0.4
 # cons_to_prim/time_step arithmetic with a counting scalar (oracle/count_flops.cpp).
 FLOPS_PER_CELL_DEFAULT = None
 
+# DRAM bytes (read + write) per interior cell of the fused FP64 kernel, from
+# one ncu capture at 192^3 (profiles/flux_step_f64_192.md: 673 MB + 582 MB over
+# 7.08 M interior cells); the kernel streams each plane once, so traffic
+# scales with cells.
+FLUX_F64_DRAM_BYTES_PER_CELL = 177.3
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -612,7 +618,10 @@ def run_ours(args):
                            "the probe itself runs the FP64 pipe at ~84% of ncu's nominal 2 DFMA/clk/SM",
             "peak_nominal": nominal / 1e12,
             "kernel": "flux_tile_kernel<double, step>", "kernel_ms": flux_ms,
-            "step_ms_sum_of_launches": step_ms_launches, "traffic": None}
+            "step_ms_sum_of_launches": step_ms_launches,
+            "traffic": FLUX_F64_DRAM_BYTES_PER_CELL * interior,
+            "traffic_note": "dram bytes read+write per launch: 177.3 B per interior cell from an ncu capture at "
+                            "192^3 (profiles/flux_step_f64_192.md), scaled by cells"}
     if fpc:
         fl = fpc["fused_step_fp64"] * interior
         roof["achieved"] = fl / (flux_ms * 1e-3) / 1e12
