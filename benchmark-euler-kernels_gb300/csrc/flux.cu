@@ -767,7 +767,12 @@ template <class T>
 __device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time, const double* dt_seq = nullptr)
 {
     if (add_time) {
-        s->t += dt_seq != nullptr ? dt_seq[s->steps] : static_cast<double>(cfl * static_cast<T>(s->dt));
+        // the step just taken, cfl*dt (or the fixed dt), added with separate
+        // roundings (no FMA) so every kernel that inlines this agrees bit for bit
+        double const step = dt_seq != nullptr ? dt_seq[s->steps]
+                                              : (sizeof(T) == 8 ? __dmul_rn(static_cast<double>(cfl), s->dt)
+                                                                : static_cast<double>(cfl * static_cast<T>(s->dt)));
+        s->t = __dadd_rn(s->t, step);
         s->steps += 1;
     }
     T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(s->wmax)));

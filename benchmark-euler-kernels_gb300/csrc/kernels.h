@@ -99,6 +99,10 @@ cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1
                              int sms, cudaStream_t s);
 template <class T>
 cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s);
+// prim_to_cons (when cons.f[0] is set) + sound speed + max wavespeed in one pass.
+template <class T>
+cudaError_t launch_load_prim(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma, T ix0, T ix1, T ix2,
+                             unsigned long long* wmax, int sms, cudaStream_t s);
 cudaError_t launch_init_step(Bundle<double> prim, Geom g, double dx0, double dx1, double dx2, double c,
                              double rho_in, double p_in, double rho_out, double p_out, int sms, cudaStream_t s);
 // max invdt over all cells of a cons-only FP32 state (compensated: FP64

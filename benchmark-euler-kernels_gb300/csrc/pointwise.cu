@@ -208,6 +208,53 @@ __global__ void __launch_bounds__(256) invdt_max_cons_kernel(CBundle<float> cons
     }
 }
 
+// Loading a primitive state into an FP64 simulation, in one pass: cons =
+// prim_to_cons(prim) (when cons is set; as prim_to_cons_kernel), the stored
+// sound speed (as sound_speed_kernel) and the max wavespeed of the first
+// step (as invdt_max_kernel) -- bit-identical to the three kernels run one
+// after the other.
+template <class T>
+__global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma,
+                                                        T gm1, T rgm1, T ix0, T ix1, T ix2, unsigned long long* wmax)
+{
+    T local = T(0);
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        T const d = prim.f[0][c];
+        T const p = prim.f[1][c];
+        T const u0 = prim.f[2][c];
+        T const u1 = prim.f[3][c];
+        T const u2 = prim.f[4][c];
+        if (cons.f[0] != nullptr) {
+            T const int_e = div_by_rcp(p, gm1, rgm1);
+            T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
+            cons.f[0][c] = d;
+            cons.f[1][c] = add_rn(ke, int_e);
+            cons.f[2][c] = mul_rn(d, u0);
+            cons.f[3][c] = mul_rn(d, u1);
+            cons.f[4][c] = mul_rn(d, u2);
+        }
+        T const sc = sqrt_rn(div_rn(mul_rn(gamma, p), d));
+        cs[c] = sc;
+        T const v = add_rn(add_rn(mul_rn(add_rn(sc, abs_(u0)), ix0), mul_rn(add_rn(sc, abs_(u1)), ix1)),
+                           mul_rn(add_rn(sc, abs_(u2)), ix2));
+        local = (v > local) ? v : local;
+    }
+    __shared__ T warp_best[8];
+    local = warp_max(local);
+    if ((threadIdx.x & 31) == 0) {
+        warp_best[threadIdx.x >> 5] = local;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T b = warp_best[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            b = (warp_best[w] > b) ? warp_best[w] : b;
+        }
+        atomicMax(wmax, order_bits(b));
+    }
+}
+
 // Sound speed sqrt((gamma p)/d) of every cell (perfect_gas.hpp:15-18).
 template <class T>
 __global__ void __launch_bounds__(256) sound_speed_kernel(CBundle<T> prim, T* cs, long long n, T gamma)
@@ -297,6 +344,16 @@ cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1
 }
 
 template <class T>
+cudaError_t launch_load_prim(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma, T ix0, T ix1, T ix2,
+                             unsigned long long* wmax, int sms, cudaStream_t s)
+{
+    T const gm1 = gamma - T(1);
+    load_prim_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cons, cs, n, gamma, gm1, T(1) / gm1, ix0, ix1, ix2,
+                                                          wmax);
+    return cudaGetLastError();
+}
+
+template <class T>
 cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s)
 {
     sound_speed_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cs, n, gamma);
@@ -326,7 +383,9 @@ cudaError_t launch_invdt_max_cons(CBundle<float> cons, long long n, float gamma,
                                              int, cudaStream_t);                                             \
     template cudaError_t launch_invdt_max<T>(CBundle<T>, long long, T, T, T, T, unsigned long long*, int,    \
                                              cudaStream_t);                                                  \
-    template cudaError_t launch_sound_speed<T>(CBundle<T>, T*, long long, T, int, cudaStream_t);
+    template cudaError_t launch_sound_speed<T>(CBundle<T>, T*, long long, T, int, cudaStream_t);                   \
+    template cudaError_t launch_load_prim<T>(CBundle<T>, Bundle<T>, T*, long long, T, T, T, T, unsigned long long*,    \
+                                             int, cudaStream_t);
 
 EULR_INSTANTIATE_POINTWISE(double)
 EULR_INSTANTIATE_POINTWISE(float)

@@ -292,18 +292,24 @@ int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
 
 // After a state was loaded into copy 0: sound speed (FP64 state), dt of the
 // state, zeroed clock and status.
-int prepare_loaded(eulr_sim* s)
+// Resets the clocks of copy 0 and computes its first dt.  FP64: with
+// derive_cons, cons = prim_to_cons(prim) is computed in the same pass as the
+// sound speed and the wavespeed (launch_load_prim); otherwise cons is taken
+// as loaded.
+int prepare_loaded(eulr_sim* s, bool derive_cons = false)
 {
     s->cur = 0;
     s->host_steps = 0;
     SIM_CUDA(cudaMemsetAsync(s->sc, 0, sizeof(SimScalars), s->stream), "cudaMemsetAsync");
     if (is_f64(s)) {
         CBundle<double> pv = cbundle_of<double>(s->prim[0]);
-        SIM_CUDA(launch_sound_speed<double>(pv, static_cast<double*>(s->cs[0]), ncell(s), s->gamma, s->sms, s->stream),
-                 "sound speed launch");
-        SIM_CUDA(launch_invdt_max<double>(pv, ncell(s), s->gamma, 1.0 / s->dx[0], 1.0 / s->dx[1], 1.0 / s->dx[2],
-                                          &s->sc->wmax, s->sms, s->stream),
-                 "invdt launch");
+        Bundle<double> cv{};
+        if (derive_cons) {
+            cv = bundle_of<double>(s->cons[0]);
+        }
+        SIM_CUDA(launch_load_prim<double>(pv, cv, static_cast<double*>(s->cs[0]), ncell(s), s->gamma, 1.0 / s->dx[0],
+                                          1.0 / s->dx[1], 1.0 / s->dx[2], &s->sc->wmax, s->sms, s->stream),
+                 "load launch");
         SIM_CUDA(launch_finalize_dt<double>(s->sc, s->cfl, 0, s->stream), "finalize launch");
     } else {
         float const g = static_cast<float>(s->gamma);
@@ -377,13 +383,8 @@ int set_state_impl(eulr_sim* s, const double* const* prim, const double* const* 
         SIM_TRY(copy_in(s, s->prim[0], prim));
         if (cons != nullptr) {
             SIM_TRY(copy_in(s, s->cons[0], cons));
-        } else {
-            double const gm1 = s->gamma - 1.0;
-            SIM_CUDA(launch_prim_to_cons<double>(cbundle_of<double>(s->prim[0]), bundle_of<double>(s->cons[0]),
-                                                 ncell(s), gm1, 1.0 / gm1, s->sms, s->stream),
-                     "prim_to_cons");
         }
-        return prepare_loaded(s);
+        return prepare_loaded(s, cons == nullptr);
     }
     Staging st;
     SIM_TRY(make_staging(s, st, cons != nullptr ? 10 : 5));
@@ -612,11 +613,7 @@ int eulr_sim_init_implode(eulr_sim* s)
         SIM_CUDA(launch_init_implode<double>(bundle_of<double>(s->prim[0]), s->g, s->dx[0], s->dx[1], s->dx[2], s->sms,
                                              s->stream),
                  "init_implode");
-        double const gm1 = s->gamma - 1.0;
-        SIM_CUDA(launch_prim_to_cons<double>(cbundle_of<double>(s->prim[0]), bundle_of<double>(s->cons[0]), ncell(s),
-                                             gm1, 1.0 / gm1, s->sms, s->stream),
-                 "prim_to_cons");
-        return prepare_loaded(s);
+        return prepare_loaded(s, true);
     }
     // FP32 states: the FP64 implosion state, converted on the device
     Staging st;
@@ -720,6 +717,33 @@ int eulr_sim_get_state_f64(eulr_sim* s, eulr_prim_f64 prim, eulr_cons_f64 cons)
         }
     }
     SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize"); // staging is freed next
+    return EULR_SUCCESS;
+}
+
+int eulr_sim_get_state_async_f64(eulr_sim* s, eulr_prim_f64 prim, eulr_cons_f64 cons)
+{
+    SIM_TRY(check_sim(s));
+    if (!is_f64(s)) {
+        return eulr::sim_fail(EULR_ERR_UNSUPPORTED, "asynchronous state reads need an FP64 simulation");
+    }
+    size_t const bytes = static_cast<size_t>(ncell(s)) * sizeof(double);
+    double* pf[5] = {prim.d, prim.p, prim.ux0, prim.ux1, prim.ux2};
+    double* cf[5] = {cons.d, cons.e, cons.mx0, cons.mx1, cons.mx2};
+    for (int i = 0; i < 5; ++i) {
+        if (pf[i] != nullptr) {
+            SIM_CUDA(cudaMemcpyAsync(pf[i], s->prim[s->cur][i], bytes, cudaMemcpyDefault, s->stream), "copy out");
+        }
+        if (cf[i] != nullptr) {
+            SIM_CUDA(cudaMemcpyAsync(cf[i], s->cons[s->cur][i], bytes, cudaMemcpyDefault, s->stream), "copy out");
+        }
+    }
+    return EULR_SUCCESS;
+}
+
+int eulr_sim_synchronize(eulr_sim* s)
+{
+    SIM_TRY(check_sim(s));
+    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
     return EULR_SUCCESS;
 }
 

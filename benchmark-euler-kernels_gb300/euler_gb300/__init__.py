@@ -73,6 +73,8 @@ _SIGNATURES = [
     ("eulr_sim_advance", _I, [_P, _I]),
     ("eulr_sim_set_dt_sequence", _I, [_P, ctypes.POINTER(_D), ctypes.c_longlong]),
     ("eulr_sim_get_state_f64", _I, [_P, Bundle5, Bundle5]),
+    ("eulr_sim_get_state_async_f64", _I, [_P, Bundle5, Bundle5]),
+    ("eulr_sim_synchronize", _I, [_P]),
     ("eulr_sim_time", _I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_longlong)]),
     ("eulr_sim_status", _I, [_P]),
     ("eulr_sim_launches_per_step", _I, [_P]),
@@ -288,10 +290,15 @@ class Simulation:
         arr = (ctypes.c_double * len(dts))(*[float(v) for v in dts])
         check(load().eulr_sim_set_dt_sequence(self._h, arr, len(dts)))
 
-    def get_state(self, prim=None, cons=None):
-        """Copy the state into the given bundles (host numpy or device tensors)."""
-        check(load().eulr_sim_get_state_f64(self._h, bundle(prim) if prim is not None else null_bundle(),
-                                            bundle(cons) if cons is not None else null_bundle()))
+    def get_state(self, prim=None, cons=None, wait=True):
+        """Copy the state into the given bundles (host numpy or device tensors).
+        With wait=False (FP64) the copies are only enqueued; see synchronize()."""
+        fn = load().eulr_sim_get_state_f64 if wait else load().eulr_sim_get_state_async_f64
+        check(fn(self._h, bundle(prim) if prim is not None else null_bundle(),
+                 bundle(cons) if cons is not None else null_bundle()))
+
+    def synchronize(self):
+        check(load().eulr_sim_synchronize(self._h))
 
     def state_numpy(self):
         import numpy as np

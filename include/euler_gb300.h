@@ -219,9 +219,11 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
 int eulr_sim_destroy(eulr_sim* sim);
 
 /* Load the state.  Pointers may be host or device memory (copies use
- * cudaMemcpyDefault).  set_prim computes cons = prim_to_cons(prim), as the
- * reference driver does after init (euler_simulation.cpp:50-51);
- * set_state takes both bundles as they are. */
+ * cudaMemcpyDefault); loading is asynchronous for FP64 simulations.
+ * set_prim computes cons = prim_to_cons(prim), as the reference driver does
+ * after init (euler_simulation.cpp:50-51); set_state takes both bundles as
+ * they are.  Host sources must stay unchanged until the stream has consumed
+ * them (eulr_sim_synchronize, or the next waiting call). */
 int eulr_sim_set_prim_f64(eulr_sim* sim, eulr_prim_cf64 prim);
 int eulr_sim_set_state_f64(eulr_sim* sim, eulr_prim_cf64 prim, eulr_cons_cf64 cons);
 /* init_implode + prim_to_cons on the device. */
@@ -240,6 +242,15 @@ int eulr_sim_set_dt_sequence(eulr_sim* sim, const double* dts, long long n);
 /* Copy the current state out (host or device destination); waits for the
  * stream.  Either bundle pointer set may be all-NULL to skip it. */
 int eulr_sim_get_state_f64(eulr_sim* sim, eulr_prim_f64 prim, eulr_cons_f64 cons);
+
+/* As eulr_sim_get_state_f64 for an FP64 simulation, without waiting: the
+ * copies are enqueued on the simulation's stream (a later set/advance on the
+ * same simulation is ordered after them).  Host destinations should be
+ * pinned for the copies to be asynchronous.  EULR_ERR_UNSUPPORTED for FP32
+ * states. */
+int eulr_sim_get_state_async_f64(eulr_sim* sim, eulr_prim_f64 prim, eulr_cons_f64 cons);
+/* Waits for all work enqueued on the simulation's stream. */
+int eulr_sim_synchronize(eulr_sim* sim);
 
 /* Simulated time (sum of cfl*dt over the steps taken), the dt of the next
  * step, and the number of steps taken; waits for the stream. */

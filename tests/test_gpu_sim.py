@@ -136,3 +136,29 @@ def test_nonphysical_state_is_reported(cuda, euler, oracle_lib):
         sim.set_prim(prim0)
         sim.advance(2)
         assert sim.status() == -7  # EULR_ERR_NONFINITE
+
+
+def test_async_state_read_and_fused_load(cuda, euler, oracle_lib):
+    """set_prim's one-pass load (prim_to_cons + sound speed + first dt) and the
+    asynchronous read agree with the oracle and with the waiting read."""
+    torch, O = cuda, oracle_lib
+    prim = O.random_prim(20, 18, 16, seed=7)
+    gamma, dx = 1.4, (0.05, 0.06, 0.07)
+    cons_ref = O.prim_to_cons(prim, gamma)
+    dt_ref = 0.4 * O.time_step(prim, gamma, dx)
+    host = torch.from_numpy(prim).pin_memory()
+    with euler.Simulation(20, 18, 16, gamma, dx, 0.4) as sim:
+        sim.set_prim(host)
+        p, c = sim.state_numpy()
+        assert np.array_equal(c, cons_ref) and np.array_equal(p, prim)
+        assert sim.time()[1] == dt_ref
+        sim.advance(3)
+        a = torch.empty((5, 16, 18, 20), dtype=torch.float64).pin_memory()
+        sim.get_state(prim=a, wait=False)
+        sim.synchronize()
+        b, _ = sim.state_numpy()
+        assert np.array_equal(a.numpy(), b)
+    with euler.Simulation(20, 18, 16, gamma, dx, 0.4, precision="f32c") as sim:
+        sim.set_prim(host)
+        with pytest.raises(euler.EulerError):
+            sim.get_state(prim=torch.empty((5, 16, 18, 20), dtype=torch.float64), wait=False)
