@@ -506,8 +506,11 @@ def run_batch_leg(torch, E, stream, args, precision):
             "grid0_t": t0[0]}
 
 
-def time_ops(torch, E, prim, n_int):
-    """Each reference operator alone, one call after warm-up (CUDA events)."""
+def time_ops(torch, E, prim, n_int, fpc=None, fp64_peak=None, hbm_peak=None):
+    """Each reference operator alone, one call after warm-up (CUDA events),
+    with its HBM and FP64 rooflines: the reference's byte counters and the
+    algorithmic FLOPs per cell of oracle/flops_per_cell.json (godunov: 3 faces
+    per interior cell, each face solved once)."""
     n0 = n_int + 2
     dx = (1.0 / n_int,) * 3
     cons = E.prim_to_cons(prim, GAMMA)
@@ -542,6 +545,19 @@ def time_ops(torch, E, prim, n_int):
     out["godunov"] = {"ms": ms, "gcells_s": cells / ms / 1e6, "gb_s": 120 * cells / ms / 1e6,
                       "interior_gcells_s": interior / ms / 1e6}
     del cons, prim2
+    if fpc:
+        flops = {"prim_to_cons": (fpc["prim_to_cons_per_cell"]["total"], cells),
+                 "cons_to_prim": (fpc["cons_to_prim_per_cell"]["total"], cells),
+                 "time_step": (fpc["time_step_per_cell"]["total"], cells),
+                 "godunov": (3 * fpc["hllc_face"]["total"] + fpc["godunov_update_per_cell"]["total"], interior)}
+        for name, (per_cell, units) in flops.items():
+            rec = out[name]
+            rec["flops_per_cell"] = per_cell
+            rec["fp64_tflops"] = per_cell * units / (rec["ms"] * 1e-3) / 1e12
+            if fp64_peak:
+                rec["fp64_frac"] = rec["fp64_tflops"] * 1e12 / fp64_peak
+            if hbm_peak:
+                rec["hbm_frac"] = rec["gb_s"] / hbm_peak
     return out
 
 
@@ -660,7 +676,7 @@ def run_ours(args):
     ops = None
     if not args.no_ops and rank == 0:
         prim = random_prim_device(torch, n0, n0, n0, seed=1)
-        ops = time_ops(torch, E, prim, n)
+        ops = time_ops(torch, E, prim, n, fpc, peak, hbm_peak)
         del prim
         torch.cuda.empty_cache()
 
@@ -687,13 +703,12 @@ def run_ours(args):
         t0 = time.perf_counter()
         for step in range(args.e2e_steps):
             sm = sims[step % 2]
-            if step >= 2:
-                sm.synchronize()  # the result of step-2 is in host memory
             sm.set_prim(host)
             sm.advance(1)
             sm.get_state(prim=outs[step % 2], wait=False)
-        for sm in sims:
-            sm.synchronize()
+            if step >= 1:
+                sims[(step - 1) % 2].synchronize()  # the result of step-1 is in host memory
+        sims[(args.e2e_steps - 1) % 2].synchronize()
         el = time.perf_counter() - t0
         for sm in sims:
             sm.close()

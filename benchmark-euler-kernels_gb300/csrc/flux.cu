@@ -187,7 +187,7 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
                 T const m2 = __ldg(p.cons_in.f[4] + o);
                 d = __ldg(p.cons_in.f[0] + o);
                 e = __ldg(p.cons_in.f[1] + o);
-                T const r = T(1) / d;
+                T const r = rcp_rn(d); // = 1/d correctly rounded, without the division routine
                 u0 = m0 * r;
                 u1 = m1 * r;
                 u2 = m2 * r;
@@ -274,7 +274,8 @@ struct TileCtx {
     unsigned phase;           // bit s: parity of slot s's next completion (TMA ring)
     unsigned inflight;        // bit s: a TMA into slot s has not been waited for
     bool timed_out;           // a bounded mbarrier wait ran out
-    long long wkey;           // ordered bits of this thread's max wavespeed
+    long long wkey;           // ordered bits of this thread's max wavespeed (FP64)
+    float wmaxf;              // this thread's max wavespeed (FP32 states: keyed once, at the flush)
     bool bad;                 // this thread saw a non-physical cell
 };
 
@@ -477,8 +478,12 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
                 }
                 // next step's CFL wavespeed (time_step.hpp:28-33)
                 T const invdt = (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
-                long long const key = wave_key(invdt);
-                c.wkey = key > c.wkey ? key : c.wkey;
+                if constexpr (sizeof(T) == 4) {
+                    c.wmaxf = fmaxf(c.wmaxf, invdt); // NaN never wins (fmaxf returns the other operand)
+                } else {
+                    long long const key = wave_key(invdt);
+                    c.wkey = key > c.wkey ? key : c.wkey;
+                }
                 c.bad |= !cell_ok(u[0], pr, invdt);
             }
         }
@@ -501,6 +506,10 @@ __device__ __forceinline__ void flush_wavespeed(TileCtx<T>& c, unsigned long lon
     __shared__ int any_bad;
     int const tid = threadIdx.x;
     long long w = c.wkey;
+    if constexpr (sizeof(T) == 4) {
+        long long const kf = wave_key(c.wmaxf);
+        w = kf > w ? kf : w;
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         long long const v = __shfl_xor_sync(0xffffffffu, w, o);
@@ -530,6 +539,7 @@ __device__ __forceinline__ void flush_wavespeed(TileCtx<T>& c, unsigned long lon
         }
     }
     c.wkey = 0;
+    c.wmaxf = 0.0f;
     c.bad = false;
 }
 
@@ -549,6 +559,7 @@ __device__ __forceinline__ TileCtx<T> make_ctx(unsigned char* smem_dyn)
     c.inflight = 0;
     c.timed_out = false;
     c.wkey = 0;
+    c.wmaxf = 0.0f;
     c.bad = false;
     return c;
 }
