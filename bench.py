@@ -100,6 +100,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float, device="cpu") -> float:
+    """The largest of every rank's value (the slowest rank's time); the
+    value itself with one process."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells_per_rank: int, steps: int, world: int, ms_max: float) -> float:
+    """Whole-job Gcell-updates/s of `world` replicas that each update
+    `cells_per_rank` cells per step, timed by the slowest rank."""
+    return world * cells_per_rank * steps / (ms_max * 1e-3) / 1e9
+
+
 def flops_per_cell():
     path = os.path.join(ROOT, "oracle", "flops_per_cell.json")
     if os.path.exists(path):
@@ -197,18 +216,50 @@ def cpu_baseline(n: int, seconds: float):
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU implementation of the path (the
+    oracle port: the reference's own sources are not present on the GPU host)
+    on all host cores.  A step is one step of the reference loop (time_step,
+    godunov, cons_to_prim) on an n x n x kz-interior slab of the same random
+    state, kz sized so that --warmup + --steps steps take about --cpu-seconds.
+    Under torchrun only rank 0 works and prints; the other ranks exit 0."""
+    import numpy as np
+
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    res = cpu_baseline(args.n, args.cpu_seconds)
+    import oracle as O
+
+    O.build(ref=False)
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    n = args.n
+    dx = (1.0 / n,) * 3
+    probe = O.random_prim(n + 2, n + 2, 3, seed=0)
+    pc = O.prim_to_cons(probe, GAMMA)
+    t0 = time.perf_counter()
+    O.simulate(probe, pc, GAMMA, dx, CFL, 1)
+    per_plane = max(time.perf_counter() - t0, 1e-6)
+    nsteps = args.warmup + args.steps
+    kz = int(max(1, min(n, args.cpu_seconds / nsteps / per_plane)))
+    prim = O.random_prim(n + 2, n + 2, kz + 2, seed=0)
+    cons = O.prim_to_cons(prim, GAMMA)
+    O.simulate(prim, cons, GAMMA, dx, CFL, args.warmup)
+    t0 = time.perf_counter()
+    O.simulate(prim, cons, GAMMA, dx, CFL, args.steps)
+    el = time.perf_counter() - t0
+    value = n * n * kz * args.steps / el / 1e9
+    sample = (f"{args.steps} timed steps (after {args.warmup} warm-up) of the reference loop on a "
+              f"{n}x{n}x{kz}-interior slab of the {n}^3 workload's random state, {el:.1f} s")
     line = {
-        "impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"fused Euler step, {args.n}^3 interior, seeded random state", "n": args.n,
-                   "l2": "inputs larger than L2"},
-        "cpu_baseline": {k: v for k, v in res.items() if not k.startswith("_")},
-        "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"fused Euler step, {n}^3 interior, seeded random state (rho, p log-uniform "
+                               "[0.1,10], u ~ N(0,1)), gamma 1.4, CFL 0.4", "n": n,
+                   "l2": "CPU run (no GPU caches involved)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                         "numpy": np.__version__},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference arm: the reference's CPU implementation of the path, as the oracle port (the "
                 "reference sources are not present on the GPU host); OpenMP over all host cores",
     }
@@ -613,13 +664,9 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    ms = s.elapsed_time(e)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = t.item()
+    ms = max_over_ranks(s.elapsed_time(e), device="cuda")
     ms_per_step = ms / args.steps
-    value = world * interior * args.steps / (ms * 1e-3) / 1e9
+    value = replica_throughput(interior, args.steps, world, ms)
     status = sim.status()
     t_sim, next_dt, nsteps = sim.time()
     launches = args.steps * sim.launches_per_step()

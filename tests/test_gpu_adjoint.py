@@ -282,3 +282,30 @@ def test_differentiation_workload_full(cuda, euler, oracle_lib):
         "fd_max_err_over_rms": max(abs(f - g) for g, f, _ in rows) / rms}}
     print(json.dumps(rec))
     assert abs(a - tlm) <= 1e-6 * abs(tlm)
+
+
+def test_ragged_anisotropic_grid_and_all_fields(cuda, euler, oracle_lib):
+    """Odd, unequal extents (the forward step's plain-load path), unequal
+    spacings, a generic moving state, a cotangent on every final field, and
+    a direction in all five initial fields."""
+    torch, O = cuda, oracle_lib
+    n0, n1, n2 = 21, 17, 13
+    dx = (0.05, 0.07, 0.06)
+    prim0 = O.random_prim(n0, n1, n2, seed=13)
+    prim0[2:] *= 0.3
+    nsteps = 8
+    adj = euler.Adjoint(n0, n1, n2, nsteps, gamma=1.3, dx=dx, checkpoint_every=3)
+    out = torch.empty((5, n2, n1, n0), dtype=torch.float64, device="cuda")
+    adj.forward(torch.from_numpy(prim0).cuda(), out=out)
+    dts = adj.dts()
+    rng = np.random.default_rng(21)
+    wT = rng.normal(size=prim0.shape)
+    g0 = torch.empty_like(out)
+    adj.backward(torch.from_numpy(wT).cuda(), g0)
+    grad = g0.cpu().numpy()
+    for _ in range(3):
+        v = rng.normal(size=prim0.shape)
+        _, dT = O.tlm_simulate(prim0, v, 1.3, dx, dts)
+        ref = float(np.sum(wT * dT))
+        got = float(np.sum(grad * v))
+        assert abs(got - ref) <= 1e-10 * abs(ref), (got, ref)
