@@ -217,7 +217,7 @@ def cpu_baseline(n: int, seconds: float):
 
 def run_reference(args):
     """The reference arm: the reference's CPU implementation of the path (the
-    oracle port: the reference's own sources are not present on the GPU host)
+    oracle port: the reference's own sources are not present where this runs)
     on all host cores.  A step is one step of the reference loop (time_step,
     godunov, cons_to_prim) on an n x n x kz-interior slab of the same random
     state, kz sized so that --warmup + --steps steps take about --cpu-seconds.
@@ -261,7 +261,7 @@ def run_reference(args):
                          "numpy": np.__version__},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference arm: the reference's CPU implementation of the path, as the oracle port (the "
-                "reference sources are not present on the GPU host); OpenMP over all host cores",
+                "reference sources are not present where this runs); OpenMP over all host cores",
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -1,8 +1,9 @@
 """CPU oracle for the Euler operators -- TEST INFRASTRUCTURE ONLY.
 
-Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use this module, and only as the checker or as the timed CPU
-baseline.  The product path (the CUDA library) never imports it.
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg and
+reference arm of ``bench.py`` use this module, and only as the parity
+reference or as the timed CPU baseline.  The product path (the CUDA library)
+never imports it.
 
 Two implementations sit behind the same numpy interface:
 

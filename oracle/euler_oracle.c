@@ -1,7 +1,7 @@
 /* CPU oracle for the Euler operators (TEST INFRASTRUCTURE ONLY).
  *
  * A plain-C restatement of the reference operator headers (euler_operators/), used by the
- * tests, the smoke check and bench.py's CPU-baseline leg as the checker.  It is
+ * tests, the smoke check and bench.py's CPU-baseline leg as the parity reference.  It is
  * pinned bit-for-bit against the reference itself (oracle/_ref, built from the
  * reference headers by oracle/Makefile) and against the golden fixtures under
  * tests/golden/.  Build: see oracle/Makefile (-O2 -ffp-contract=off -fopenmp).

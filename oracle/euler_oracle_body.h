@@ -1,7 +1,7 @@
 /* CPU oracle: C restatement of the reference's Euler operators.
  *
  * TEST INFRASTRUCTURE ONLY.  Tests, the smoke check and the CPU-baseline leg
- * of bench.py use this code as the checker; the product path never calls it.
+ * of bench.py use this code as the parity reference; the product path never calls it.
  *
  * Included twice by euler_oracle.c, once with REAL=double / SUF=f64 and once
  * with REAL=float / SUF=f32 (the reference's real_t switch,

@@ -2,7 +2,7 @@
 //
 // This is test infrastructure, not product code: it exists so that the
 // reference's header-only operators (euler_operators/*.hpp) compile unmodified
-// with plain g++ and OpenMP, producing the checker that pins the C restatement
+// with plain g++ and OpenMP, producing the reference build that pins the C restatement
 // in oracle/euler_oracle.c.  It implements only the subset of the Kokkos API
 // those headers touch:
 //   mdspan / extents / dextents / layout_left / layout_right / default_accessor

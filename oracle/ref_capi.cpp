@@ -5,7 +5,7 @@
 // time_step,prim_to_cons,cons_to_prim,init_implode}.hpp) UNMODIFIED, compiled
 // against the Kokkos compatibility layer in oracle/kokkos_compat, and exposes
 // them as plain C functions over host arrays.  The recipe in oracle/Makefile
-// builds it into oracle/_ref/libeuler_ref.so.  It is the checker that pins the
+// builds it into oracle/_ref/libeuler_ref.so.  It is the reference build that pins the
 // C restatement (oracle/euler_oracle.c) and generates the committed golden
 // fixtures; it is never part of the product.
 //
