@@ -287,7 +287,8 @@ __device__ __forceinline__ Flux<float> hllc_flux(Side<float> const& L, Side<floa
     float const qe = left ? L.e : R.e;
     float const qrc = left ? rc_L : rc_R;
     float const M = S * den - num;
-    float const Rr = __frcp_rn(den * M);
+    float const Rr = __fdividef(1.0f, den * M); // hardware reciprocal (<= 2 ulp): |den M| is far from the
+                                                 // ends of the float range for any physical state
     float const ustar = num * (M * Rr);
     float const inv = den * (den * Rr);
     float const w = ustar - qun;
