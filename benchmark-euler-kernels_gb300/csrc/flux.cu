@@ -940,6 +940,39 @@ __device__ __forceinline__ Raw5 load_raw(FluxParams<float> const& p, int i, int 
     return r;
 }
 
+// Asynchronous 4-byte global->shared copies (cp.async): the prefetched cons
+// of the next planes wait in shared memory instead of registers.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Starts copying the cons of cell (i, j, k) to dst[f * stride] (benign values for cells outside the array).
+__device__ __forceinline__ void prefetch_raw(float* dst, int stride, FluxParams<float> const& p, int i, int j, int k)
+{
+    if (i >= p.g.n0 || j >= p.g.n1) {
+        Raw5 const b = outside();
+        dst[0] = b.d;
+        dst[stride] = b.e;
+        dst[2 * stride] = b.m[0];
+        dst[3 * stride] = b.m[1];
+        dst[4 * stride] = b.m[2];
+        return;
+    }
+    long long const o = p.g.at(i, j, k);
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+        cp_async4(dst + f * stride, p.cons_in.f[f] + o);
+    }
+}
+
+__device__ __forceinline__ Raw5 read_raw(float const* src, int stride)
+{
+    return Raw5{src[0], src[stride], {src[2 * stride], src[3 * stride], src[4 * stride]}};
+}
+
 __device__ __forceinline__ void halo_cell(int h, int& hx, int& hy)
 {
     if (h < TY) {
@@ -996,6 +1029,8 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
     static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
     __shared__ __align__(16) float slot[2][kFields * PLANE];
     __shared__ __align__(16) float yflux[5][NT];
+    __shared__ __align__(16) float raw_own[5 * NT];     // own column, two planes ahead
+    __shared__ __align__(16) float raw_halo[5 * NHALO]; // halo ring, one plane ahead
     __shared__ long long warp_best[NT / 32];
     __shared__ int any_bad;
 
@@ -1025,13 +1060,12 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
 
         // prologue: planes kb-1 (z face below), kb, kb+1 of the own column,
         // plane kb of the halo ring
+        if (tid < NHALO) {
+            prefetch_raw(raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
+        }
         Raw5 const rb = load_raw(p, i, j, kb - 1);
         Raw5 rk = load_raw(p, i, j, kb);
         Raw5 rn = load_raw(p, i, j, kb + 1); // kb + 1 <= ke <= n2 - 1
-        Raw5 rh{};
-        if (tid < NHALO) {
-            rh = load_raw(p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
-        }
         Prim7 q0 = prim_of<COMP>(rk, p);
         Prim7 q1 = prim_of<COMP>(rn, p);
         float zlo[5];
@@ -1043,15 +1077,15 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
             // stage plane k: the own cell and the halo ring
             put(q, own_idx, q0);
             if (tid < NHALO) {
-                put(q, hhy * HX + hhx, prim_of<COMP>(rh, p));
+                cp_async_wait_all(); // this thread's copies of the halo cell (plane k) landed
+                put(q, hhy * HX + hhx, prim_of<COMP>(read_raw(raw_halo + tid, NHALO), p));
+                if (k + 1 < ke) {
+                    prefetch_raw(raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 1);
+                }
             }
-            // prefetch: own column plane k+2, halo ring plane k+1
-            Raw5 rnn = outside();
+            // own column plane k+2, consumed at the end of this plane
             if (k + 2 <= ke) {
-                rnn = load_raw(p, i, j, k + 2);
-            }
-            if (tid < NHALO && k + 1 < ke) {
-                rh = load_raw(p, i0 - 1 + hhx, j0 - 1 + hhy, k + 1);
+                prefetch_raw(raw_own + tid, NT, p, i, j, k + 2);
             }
             __syncthreads(); // plane k staged
 
@@ -1140,10 +1174,11 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
                 zlo[f] = fzh[f];
             }
             rk = rn;
-            rn = rnn;
             q0 = q1;
             if (k + 2 <= ke) {
-                q1 = prim_of<COMP>(rnn, p);
+                cp_async_wait_all();
+                rn = read_raw(raw_own + tid, NT);
+                q1 = prim_of<COMP>(rn, p);
             }
             o += p.g.s2;
         }
