@@ -277,7 +277,9 @@ __device__ __forceinline__ Flux<float> hllc_flux(Side<float> const& L, Side<floa
     float const rc_R = R.d * (S_R - R.un);
     float const num = (R.p - L.p) + rc_L * L.un - rc_R * R.un;
     float const den = rc_L - rc_R;
-    bool const left = (num > 0.0f) == (den > 0.0f) && num != 0.0f && den != 0.0f;
+    // rc_L <= 0 <= rc_R (S_L - un_L <= -cmax, S_R - un_R >= cmax, and rounding is
+    // monotone), so den <= 0 and ustar = num/den > 0 exactly when num < 0
+    bool const left = num < 0.0f;
     float const S = left ? S_L : S_R;
     float const qd = left ? L.d : R.d;
     float const qp = left ? L.p : R.p;

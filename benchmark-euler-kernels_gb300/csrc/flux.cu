@@ -1023,7 +1023,7 @@ __device__ __forceinline__ void two_sum_into(float& s, float& e, float t)
     s = n;
 }
 
-template <int COMP>
+template <int COMP, bool UNIFORM>
 __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__ FluxParams<float> p)
 {
     static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
@@ -1038,8 +1038,7 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
     int const ti = tid % TX; // == lane
     int const tj = tid / TX; // == warp
     float const dtodv = dt_over_dv(p);
-    float const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2;
-    bool const uniform = (k0 == k1) && (k1 == k2);
+    float const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2; // UNIFORM: all equal
     int hhx = 0, hhy = 0;
     if (tid < NHALO) {
         halo_cell(tid, hhx, hhy);
@@ -1127,7 +1126,7 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
                 for (int f = 0; f < 5; ++f) {
                     if (COMP == kCompNone) {
                         u[f] = u[f] - k0 * (fxr[f] - fxl[f]) - k1 * (fyt[f] - fyb[f]) - k2 * (fzh[f] - zlo[f]);
-                    } else if (uniform) {
+                    } else if (UNIFORM) {
                         // sum of the six signed fluxes, exactly, then k times it, exactly
                         float S = fxl[f];
                         float eS = 0.0f;
@@ -1222,7 +1221,7 @@ template <int COMP>
 cudaError_t configure_f32col(int* per_sm)
 {
     int n = 0;
-    cudaError_t const e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_step_kernel<COMP>,
+    cudaError_t const e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_step_kernel<COMP, false>,
                                                                         f32col::NT, 0);
     *per_sm = n < 1 ? 1 : n;
     return e;
@@ -1248,7 +1247,12 @@ cudaError_t launch_f32col(FluxParams<float> p, int sms, cudaStream_t s)
     long long const nwork = static_cast<long long>(p.tiles_x) * p.tiles_y * kchunks;
     p.nwork = static_cast<int>(nwork);
     long long const grid = slots < nwork ? slots : nwork;
-    f32col::f32_step_kernel<COMP><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
+    // equal face areas (cubic cells) give equal update coefficients dt/dv * ds_d
+    if (p.ds0 == p.ds1 && p.ds1 == p.ds2) {
+        f32col::f32_step_kernel<COMP, true><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
+    } else {
+        f32col::f32_step_kernel<COMP, false><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
+    }
     return cudaGetLastError();
 }
 
