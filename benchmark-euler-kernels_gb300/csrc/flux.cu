@@ -1023,195 +1023,258 @@ __device__ __forceinline__ void two_sum_into(float& s, float& e, float t)
     s = n;
 }
 
-template <int COMP, bool UNIFORM>
-__global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__ FluxParams<float> p)
-{
-    static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
-    __shared__ __align__(16) float slot[2][kFields * PLANE];
-    __shared__ __align__(16) float yflux[5][NT];
-    __shared__ __align__(16) float raw_own[5 * NT];     // own column, two planes ahead
-    __shared__ __align__(16) float raw_halo[5 * NHALO]; // halo ring, one plane ahead
-    __shared__ long long warp_best[NT / 32];
-    __shared__ int any_bad;
+struct ColShared {
+    float slot[2][kFields * PLANE];
+    float yflux[5][NT];
+    float raw_own[5 * NT];     // own column, two planes ahead
+    float raw_halo[5 * NHALO]; // halo ring, one plane ahead
+    long long warp_best[NT / 32];
+    int any_bad;
+};
 
+// One work item: interior planes [kb, ke) of the 32 x 8 column tile (tx, ty),
+// kb = 1 + kc * kchunk, with update coefficients k0..k2 (all equal when UNIFORM).
+// Accumulates this thread's max wavespeed and non-physical flag.
+template <int COMP, bool UNIFORM>
+__device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, float k1, float k2, int tx, int ty,
+                                         int kc, ColShared& sh, float& wmaxf, bool& bad)
+{
     int const tid = threadIdx.x;
     int const ti = tid % TX; // == lane
     int const tj = tid / TX; // == warp
-    float const dtodv = dt_over_dv(p);
-    float const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2; // UNIFORM: all equal
+    int const own_idx = (tj + 1) * HX + ti + 1;
     int hhx = 0, hhy = 0;
     if (tid < NHALO) {
         halo_cell(tid, hhx, hhy);
     }
-    float wmaxf = 0.0f;
-    bool bad = false;
-    int const tiles_xy = p.tiles_x * p.tiles_y;
-    int const own_idx = (tj + 1) * HX + ti + 1;
+    int const i0 = 1 + tx * TX;
+    int const j0 = 1 + ty * TY;
+    int const kb = 1 + kc * p.kchunk;
+    int const ke = min(kb + p.kchunk, p.g.n2 - 1);
+    int const i = i0 + ti;
+    int const j = j0 + tj;
+    bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
 
-    for (int w = blockIdx.x; w < p.nwork; w += gridDim.x) {
-        int const i0 = 1 + (w % p.tiles_x) * TX;
-        int const j0 = 1 + ((w / p.tiles_x) % p.tiles_y) * TY;
-        int const kb = 1 + (w / tiles_xy) * p.kchunk;
-        int const ke = min(kb + p.kchunk, p.g.n2 - 1);
-        int const i = i0 + ti;
-        int const j = j0 + tj;
-        bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
-
-        // prologue: planes kb-1 (z face below), kb, kb+1 of the own column,
-        // plane kb of the halo ring
-        if (tid < NHALO) {
-            prefetch_raw(raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
-        }
-        Raw5 const rb = load_raw(p, i, j, kb - 1);
-        Raw5 rk = load_raw(p, i, j, kb);
-        Raw5 rn = load_raw(p, i, j, kb + 1); // kb + 1 <= ke <= n2 - 1
-        Prim7 q0 = prim_of<COMP>(rk, p);
-        Prim7 q1 = prim_of<COMP>(rn, p);
-        float zlo[5];
-        to_global(hllc_flux(side_of(prim_of<COMP>(rb, p), 2), side_of(q0, 2)), 2, zlo);
-        long long o = p.g.at(min(i, p.g.n0 - 1), min(j, p.g.n1 - 1), kb);
-
-        for (int k = kb; k < ke; ++k) {
-            float* const q = slot[(k - kb) & 1];
-            // stage plane k: the own cell and the halo ring
-            put(q, own_idx, q0);
-            if (tid < NHALO) {
-                cp_async_wait_all(); // this thread's copies of the halo cell (plane k) landed
-                put(q, hhy * HX + hhx, prim_of<COMP>(read_raw(raw_halo + tid, NHALO), p));
-                if (k + 1 < ke) {
-                    prefetch_raw(raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 1);
-                }
-            }
-            // own column plane k+2, consumed at the end of this plane
-            if (k + 2 <= ke) {
-                prefetch_raw(raw_own + tid, NT, p, i, j, k + 2);
-            }
-            __syncthreads(); // plane k staged
-
-            // ---- faces
-            float fxl[5], fyb[5], fzh[5], fxr[5], fyt[5];
-            {
-                float t[5];
-                to_global(hllc_flux(side_of(get(q, own_idx - HX), 1), side_of(q0, 1)), 1, t);
-#pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    yflux[f][tid] = t[f]; // read back after the barrier (registers are scarce here)
-                }
-            }
-            to_global(hllc_flux(side_of(get(q, own_idx - 1), 0), side_of(q0, 0)), 0, fxl);
-            to_global(hllc_flux(side_of(q0, 2), side_of(q1, 2)), 2, fzh);
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                fxr[f] = __shfl_down_sync(0xffffffffu, fxl[f], 1);
-            }
-            if (ti == TX - 1) { // the tile's right boundary face
-                to_global(hllc_flux(side_of(q0, 0), side_of(get(q, own_idx + 1), 0)), 0, fxr);
-            }
-            if (tj == TY - 1) { // the tile's top boundary faces
-                to_global(hllc_flux(side_of(q0, 1), side_of(get(q, own_idx + HX), 1)), 1, fyt);
-            }
-            __syncthreads(); // y fluxes written
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                fyb[f] = yflux[f][tid];
-                if (tj < TY - 1) {
-                    fyt[f] = yflux[f][tid + TX];
-                }
-            }
-
-            // ---- update of the own cell
-            if (own) {
-                float u[5] = {rk.d, rk.e, rk.m[0], rk.m[1], rk.m[2]};
-#pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    if (COMP == kCompNone) {
-                        u[f] = u[f] - k0 * (fxr[f] - fxl[f]) - k1 * (fyt[f] - fyb[f]) - k2 * (fzh[f] - zlo[f]);
-                    } else if (UNIFORM) {
-                        // sum of the six signed fluxes, exactly, then k times it, exactly
-                        float S = fxl[f];
-                        float eS = 0.0f;
-                        two_sum_into(S, eS, -fxr[f]);
-                        two_sum_into(S, eS, fyb[f]);
-                        two_sum_into(S, eS, -fyt[f]);
-                        two_sum_into(S, eS, zlo[f]);
-                        two_sum_into(S, eS, -fzh[f]);
-                        float const P = k0 * S;
-                        float const eP = fmaf(k0, eS, fmaf(k0, S, -P));
-                        float sum = u[f];
-                        float err = eP;
-                        two_sum_into(sum, err, P);
-                        u[f] = sum + err;
-                    } else {
-                        float sum = u[f];
-                        float err = 0.0f;
-                        compensated_add(sum, err, k0, fxl[f]);
-                        compensated_add(sum, err, -k0, fxr[f]);
-                        compensated_add(sum, err, k1, fyb[f]);
-                        compensated_add(sum, err, -k1, fyt[f]);
-                        compensated_add(sum, err, k2, zlo[f]);
-                        compensated_add(sum, err, -k2, fzh[f]);
-                        u[f] = sum + err;
-                    }
-                }
-#pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    p.cons_out.f[f][o] = u[f];
-                }
-                // next step's CFL wavespeed of the new state (time_step.hpp:28-33)
-                float const r = rcp_rn(u[0]);
-                float const v0 = u[2] * r, v1 = u[3] * r, v2 = u[4] * r;
-                float const pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1, nullptr);
-                float const cs = fast_sound_speed((p.gamma * r) * pr);
-                float const invdt = (cs + fabsf(v0)) * p.invdx0 + (cs + fabsf(v1)) * p.invdx1 +
-                                    (cs + fabsf(v2)) * p.invdx2;
-                wmaxf = fmaxf(wmaxf, invdt); // NaN never wins
-                bad |= !cell_ok(u[0], pr, invdt);
-            }
-            // march: plane k+1 becomes the current plane
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                zlo[f] = fzh[f];
-            }
-            rk = rn;
-            q0 = q1;
-            if (k + 2 <= ke) {
-                cp_async_wait_all();
-                rn = read_raw(raw_own + tid, NT);
-                q1 = prim_of<COMP>(rn, p);
-            }
-            o += p.g.s2;
-        }
-        __syncthreads(); // the slots are restaged by the next item
+    // prologue: planes kb-1 (z face below), kb, kb+1 of the own column,
+    // plane kb of the halo ring
+    if (tid < NHALO) {
+        prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
     }
+    Raw5 const rb = load_raw(p, i, j, kb - 1);
+    Raw5 rk = load_raw(p, i, j, kb);
+    Raw5 rn = load_raw(p, i, j, kb + 1); // kb + 1 <= ke <= n2 - 1
+    Prim7 q0 = prim_of<COMP>(rk, p);
+    Prim7 q1 = prim_of<COMP>(rn, p);
+    float zlo[5];
+    to_global(hllc_flux(side_of(prim_of<COMP>(rb, p), 2), side_of(q0, 2)), 2, zlo);
+    long long o = p.g.at(min(i, p.g.n0 - 1), min(j, p.g.n1 - 1), kb);
 
-    // block max of the wavespeed keys, one atomicMax per CTA; non-physical flag
+    for (int k = kb; k < ke; ++k) {
+        float* const q = sh.slot[(k - kb) & 1];
+        // stage plane k: the own cell and the halo ring
+        put(q, own_idx, q0);
+        if (tid < NHALO) {
+            cp_async_wait_all(); // this thread's copies of the halo cell (plane k) landed
+            put(q, hhy * HX + hhx, prim_of<COMP>(read_raw(sh.raw_halo + tid, NHALO), p));
+            if (k + 1 < ke) {
+                prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 1);
+            }
+        }
+        // own column plane k+2, consumed at the end of this plane
+        if (k + 2 <= ke) {
+            prefetch_raw(sh.raw_own + tid, NT, p, i, j, k + 2);
+        }
+        __syncthreads(); // plane k staged
+
+        // ---- faces
+        float fxl[5], fyb[5], fzh[5], fxr[5], fyt[5];
+        {
+            float t[5];
+            to_global(hllc_flux(side_of(get(q, own_idx - HX), 1), side_of(q0, 1)), 1, t);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                sh.yflux[f][tid] = t[f]; // read back after the barrier (registers are scarce here)
+            }
+        }
+        to_global(hllc_flux(side_of(get(q, own_idx - 1), 0), side_of(q0, 0)), 0, fxl);
+        to_global(hllc_flux(side_of(q0, 2), side_of(q1, 2)), 2, fzh);
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            fxr[f] = __shfl_down_sync(0xffffffffu, fxl[f], 1);
+        }
+        if (ti == TX - 1) { // the tile's right boundary face
+            to_global(hllc_flux(side_of(q0, 0), side_of(get(q, own_idx + 1), 0)), 0, fxr);
+        }
+        if (tj == TY - 1) { // the tile's top boundary faces
+            to_global(hllc_flux(side_of(q0, 1), side_of(get(q, own_idx + HX), 1)), 1, fyt);
+        }
+        __syncthreads(); // y fluxes written
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            fyb[f] = sh.yflux[f][tid];
+            if (tj < TY - 1) {
+                fyt[f] = sh.yflux[f][tid + TX];
+            }
+        }
+
+        // ---- update of the own cell
+        if (own) {
+            float u[5] = {rk.d, rk.e, rk.m[0], rk.m[1], rk.m[2]};
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                if (COMP == kCompNone) {
+                    u[f] = u[f] - k0 * (fxr[f] - fxl[f]) - k1 * (fyt[f] - fyb[f]) - k2 * (fzh[f] - zlo[f]);
+                } else if (UNIFORM) {
+                    // sum of the six signed fluxes, exactly, then k times it, exactly
+                    float S = fxl[f];
+                    float eS = 0.0f;
+                    two_sum_into(S, eS, -fxr[f]);
+                    two_sum_into(S, eS, fyb[f]);
+                    two_sum_into(S, eS, -fyt[f]);
+                    two_sum_into(S, eS, zlo[f]);
+                    two_sum_into(S, eS, -fzh[f]);
+                    float const P = k0 * S;
+                    float const eP = fmaf(k0, eS, fmaf(k0, S, -P));
+                    float sum = u[f];
+                    float err = eP;
+                    two_sum_into(sum, err, P);
+                    u[f] = sum + err;
+                } else {
+                    float sum = u[f];
+                    float err = 0.0f;
+                    compensated_add(sum, err, k0, fxl[f]);
+                    compensated_add(sum, err, -k0, fxr[f]);
+                    compensated_add(sum, err, k1, fyb[f]);
+                    compensated_add(sum, err, -k1, fyt[f]);
+                    compensated_add(sum, err, k2, zlo[f]);
+                    compensated_add(sum, err, -k2, fzh[f]);
+                    u[f] = sum + err;
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                p.cons_out.f[f][o] = u[f];
+            }
+            // next step's CFL wavespeed of the new state (time_step.hpp:28-33)
+            float const r = rcp_rn(u[0]);
+            float const v0 = u[2] * r, v1 = u[3] * r, v2 = u[4] * r;
+            float const pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1, nullptr);
+            float const cs = fast_sound_speed((p.gamma * r) * pr);
+            float const invdt = (cs + fabsf(v0)) * p.invdx0 + (cs + fabsf(v1)) * p.invdx1 +
+                                (cs + fabsf(v2)) * p.invdx2;
+            wmaxf = fmaxf(wmaxf, invdt); // NaN never wins
+            bad |= !cell_ok(u[0], pr, invdt);
+        }
+        // march: plane k+1 becomes the current plane
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            zlo[f] = fzh[f];
+        }
+        rk = rn;
+        q0 = q1;
+        if (k + 2 <= ke) {
+            cp_async_wait_all();
+            rn = read_raw(sh.raw_own + tid, NT);
+            q1 = prim_of<COMP>(rn, p);
+        }
+        o += p.g.s2;
+    }
+    __syncthreads(); // the slots are restaged by the next item
+}
+
+// Block max of the threads' wavespeeds into *wmax (ordered bits, one
+// atomicMax per CTA) and the non-physical flag into *status; clears both.
+__device__ __forceinline__ void col_flush(ColShared& sh, float& wmaxf, bool& bad, unsigned long long* wmax,
+                                          int* status)
+{
+    int const tid = threadIdx.x;
     long long wk = wave_key(wmaxf);
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) {
         long long const v = __shfl_xor_sync(0xffffffffu, wk, s);
         wk = v > wk ? v : wk;
     }
+    __syncthreads();
     if (tid == 0) {
-        any_bad = 0;
+        sh.any_bad = 0;
     }
     __syncthreads();
-    if (ti == 0) {
-        warp_best[tj] = wk;
+    if (tid % 32 == 0) {
+        sh.warp_best[tid / 32] = wk;
     }
     if (bad) {
-        any_bad = 1;
+        sh.any_bad = 1;
     }
     __syncthreads();
     if (tid == 0) {
-        long long b = warp_best[0];
+        long long b = sh.warp_best[0];
 #pragma unroll
         for (int v = 1; v < NT / 32; ++v) {
-            b = warp_best[v] > b ? warp_best[v] : b;
+            b = sh.warp_best[v] > b ? sh.warp_best[v] : b;
         }
-        atomicMax(p.wmax, static_cast<unsigned long long>(b));
-        if (any_bad) {
-            atomicOr(p.status, 1);
+        atomicMax(wmax, static_cast<unsigned long long>(b));
+        if (sh.any_bad) {
+            atomicOr(status, 1);
         }
+    }
+    wmaxf = 0.0f;
+    bad = false;
+}
+
+template <int COMP, bool UNIFORM>
+__global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__ FluxParams<float> p)
+{
+    static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
+    __shared__ __align__(16) ColShared sh;
+    float const dtodv = dt_over_dv(p);
+    float const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2; // UNIFORM: all equal
+    float wmaxf = 0.0f;
+    bool bad = false;
+    int const tiles_xy = p.tiles_x * p.tiles_y;
+    for (int w = blockIdx.x; w < p.nwork; w += gridDim.x) {
+        col_item<COMP, UNIFORM>(p, k0, k1, k2, w % p.tiles_x, (w / p.tiles_x) % p.tiles_y, w / tiles_xy, sh, wmaxf,
+                                bad);
+    }
+    col_flush(sh, wmaxf, bad, p.wmax, p.status);
+}
+
+// The column engine over a batch: CTAs pop (grid, tile x, tile y, chunk)
+// items from the queue, as flux_batch_kernel does; each item's wavespeed goes
+// to its own grid.  Grids with equal face areas take the cubic update.
+template <int COMP>
+__global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant__ BatchParams<float> b)
+{
+    static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
+    static_assert(sizeof(FluxParams<float>) % 4 == 0 && sizeof(FluxParams<float>) / 4 <= NT, "parameter copy");
+    __shared__ __align__(16) ColShared sh;
+    __shared__ __align__(16) FluxParams<float> gp;
+    __shared__ int s_item;
+    int const tid = threadIdx.x;
+    float wmaxf = 0.0f;
+    bool bad = false;
+    for (;;) {
+        __syncthreads(); // everyone is done with the previous item's parameters
+        if (tid == 0) {
+            s_item = static_cast<int>(atomicAdd(b.head, 1u));
+        }
+        __syncthreads();
+        int const item = s_item;
+        if (item >= b.nitems) {
+            break;
+        }
+        int4 const it = b.items[item];
+        if (tid < static_cast<int>(sizeof(FluxParams<float>) / 4)) {
+            reinterpret_cast<int*>(&gp)[tid] = reinterpret_cast<const int*>(&b.grids[it.x])[tid];
+        }
+        __syncthreads();
+        float const dtodv = dt_over_dv(gp);
+        float const k0 = dtodv * gp.ds0, k1 = dtodv * gp.ds1, k2 = dtodv * gp.ds2;
+        if (gp.ds0 == gp.ds1 && gp.ds1 == gp.ds2) {
+            col_item<COMP, true>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
+        } else {
+            col_item<COMP, false>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
+        }
+        col_flush(sh, wmaxf, bad, gp.wmax, gp.status);
     }
 }
 
@@ -1313,7 +1376,8 @@ cudaError_t launch_flux_impl(FluxParams<T> p, TmaMaps const& maps, int sms, cuda
     return cudaGetLastError();
 }
 
-// Tile shapes the batch kernel is built for (the autotuner picks one).
+// Tile shapes the batch kernel is built for (the autotuner picks one).  For
+// FP32 states without low words the 32 x 8 shape runs the column engine.
 constexpr int kBatchShapes[][2] = {{32, 8}, {16, 8}, {16, 16}};
 constexpr int kNumBatchShapes = 3;
 
@@ -1341,9 +1405,32 @@ struct BatchKernel {
     }
 };
 
+// The column engine as the 32 x 8 shape of the FP32 batch (states without low words).
+template <int COMP>
+struct ColBatchKernel {
+    static cudaError_t configure(int* per_sm)
+    {
+        int n = 0;
+        cudaError_t const e =
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_batch_kernel<COMP>, f32col::NT, 0);
+        *per_sm = n < 1 ? 1 : n;
+        return e;
+    }
+    static cudaError_t launch(BatchParams<float> const& b, int grid, cudaStream_t s)
+    {
+        f32col::f32_batch_kernel<COMP><<<grid, f32col::NT, 0, s>>>(b);
+        return cudaGetLastError();
+    }
+};
+
 template <class T, int MODE, int COMP>
 cudaError_t batch_dispatch(int shape, BatchParams<T> const* b, int grid, int* per_sm, cudaStream_t s)
 {
+    if constexpr (sizeof(T) == 4 && COMP != kCompHiLo) {
+        if (shape == 0) {
+            return b ? ColBatchKernel<COMP>::launch(*b, grid, s) : ColBatchKernel<COMP>::configure(per_sm);
+        }
+    }
     switch (shape) {
     case 0: return b ? BatchKernel<T, 32, 8, MODE, COMP>::launch(*b, grid, s) : BatchKernel<T, 32, 8, MODE, COMP>::configure(per_sm);
     case 1: return b ? BatchKernel<T, 16, 8, MODE, COMP>::launch(*b, grid, s) : BatchKernel<T, 16, 8, MODE, COMP>::configure(per_sm);

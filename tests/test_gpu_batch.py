@@ -114,3 +114,24 @@ def test_batch_rejects_bad_input(cuda, euler):
             b.advance(1)  # nothing loaded
         with pytest.raises(euler.EulerError):
             b.init_step(3, 0.2, 1, 1)  # grid index out of range
+
+
+@pytest.mark.parametrize("precision", ["f32c", "f32"])
+def test_fp32_batch_equals_single_grid_simulation(cuda, euler, precision):
+    """The FP32 batch's default 32x8 shape runs the same column engine as a
+    single FP32 simulation: bit-identical states, for cubic cells (exact
+    six-term sum) and for uneven spacings (per-term compensated sum)."""
+    import oracle as O
+
+    for grid in [(34, 26, 50, 1.3, 1 / 32, 1 / 32, 1 / 32), (34, 26, 50, 1.3, 1 / 32, 1 / 24, 1 / 48)]:
+        with euler.Batch([grid, (26, 26, 26, 1.5, 1 / 24, 1 / 24, 1 / 24)], cfl=0.4, precision=precision) as b:
+            b.init_step(0, 0.3, 0.2, 0.05)
+            b.init_step(1, 0.4, 0.5, 0.5)
+            b.advance(9)
+            pb, cb = b.state_numpy(0)
+        prim0 = O.init_step(34, 26, 50, grid[4:], 0.3, 0.2, 0.05, 1.0, 1.0)
+        with euler.Simulation(34, 26, 50, 1.3, grid[4:], 0.4, precision=precision) as s:
+            s.set_prim(prim0)
+            s.advance(9)
+            ps, cs = s.state_numpy()
+        assert np.array_equal(pb, ps) and np.array_equal(cb, cs)
