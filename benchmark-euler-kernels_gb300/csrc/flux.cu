@@ -865,7 +865,8 @@ int choose_kchunk(int columns, int iz, long long slots)
 //   * cubic cells (k0 == k1 == k2): the six fluxes are summed exactly (TwoSum
 //     chain), multiplied by k exactly (TwoProduct), and added to cons by a
 //     TwoSum, then rounded once;
-//   * otherwise each k_d F term goes through TwoProduct + TwoSum.
+//   * otherwise, per axis, the flux difference is formed exactly (TwoSum),
+//     multiplied by k_d exactly (TwoProduct) and added by a TwoSum.
 namespace f32col {
 
 constexpr int TX = 32;
@@ -1140,14 +1141,22 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
                     two_sum_into(sum, err, P);
                     u[f] = sum + err;
                 } else {
+                    // per axis: the flux difference exactly (TwoSum), times k_d exactly
+                    // (TwoProduct), into the running sum (TwoSum)
                     float sum = u[f];
                     float err = 0.0f;
-                    compensated_add(sum, err, k0, fxl[f]);
-                    compensated_add(sum, err, -k0, fxr[f]);
-                    compensated_add(sum, err, k1, fyb[f]);
-                    compensated_add(sum, err, -k1, fyt[f]);
-                    compensated_add(sum, err, k2, zlo[f]);
-                    compensated_add(sum, err, -k2, fzh[f]);
+                    float const kd[3] = {k0, k1, k2};
+                    float const lo_face[3] = {fxl[f], fyb[f], zlo[f]};
+                    float const hi_face[3] = {fxr[f], fyt[f], fzh[f]};
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        float a = lo_face[d];
+                        float ea = 0.0f;
+                        two_sum_into(a, ea, -hi_face[d]);
+                        float const P = kd[d] * a;
+                        err += fmaf(kd[d], ea, fmaf(kd[d], a, -P));
+                        two_sum_into(sum, err, P);
+                    }
                     u[f] = sum + err;
                 }
             }
