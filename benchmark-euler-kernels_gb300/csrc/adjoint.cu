@@ -54,6 +54,7 @@ struct AdjParams {
     AdjWork w;
     double gamma, gm1, inv_gm1;
     double ds[3];
+    double hds[3]; // ds / 2
     double wscale; // dt / dv
     int mode;
 };
@@ -71,35 +72,49 @@ __device__ __forceinline__ void decode(Geom const& g, long long c, int& i, int& 
     i = static_cast<int>(r - static_cast<long long>(j) * g.s1);
 }
 
+// Per-cell data of the reverse step for state `prim` at cell c (coordinates
+// i, j, k): sound speed and its derivatives, energies, 1/rho, and the face
+// weight (dt/dv) cbar on interior cells.
+__device__ __forceinline__ void prep_cell(AdjParams const& p, CBundle<double> const& prim, double wscale,
+                                          double const cb[5], long long c, int i, int j, int k)
+{
+    double const d = prim.f[0][c];
+    double const pr = prim.f[1][c];
+    double const u0 = prim.f[2][c];
+    double const u1 = prim.f[3][c];
+    double const u2 = prim.f[4][c];
+    double const R = __drcp_rn(d * pr);
+    double const inv_d = pr * R;
+    double const inv_p = d * R;
+    double const c2 = (p.gamma * pr) * inv_d;
+    double const cs = c2 * rsqrt(c2);
+    double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+    p.w.derived[0][c] = cs;
+    p.w.derived[1][c] = 0.5 * cs * inv_p;
+    p.w.derived[2][c] = -0.5 * cs * inv_d;
+    p.w.derived[3][c] = pr * p.inv_gm1 + d * ke;
+    p.w.derived[4][c] = ke;
+    p.w.derived[5][c] = inv_d;
+    bool const in = interior(p.g, i, j, k);
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+        p.w.weight[f][c] = in ? wscale * cb[f] : 0.0;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) adj_prep_kernel(AdjParams p)
 {
     long long const n = p.g.ncell();
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        double const d = p.prim.f[0][c];
-        double const pr = p.prim.f[1][c];
-        double const u0 = p.prim.f[2][c];
-        double const u1 = p.prim.f[3][c];
-        double const u2 = p.prim.f[4][c];
-        double const R = __drcp_rn(d * pr);
-        double const inv_d = pr * R;
-        double const inv_p = d * R;
-        double const c2 = (p.gamma * pr) * inv_d;
-        double const cs = c2 * rsqrt(c2);
-        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
-        p.w.derived[0][c] = cs;
-        p.w.derived[1][c] = 0.5 * cs * inv_p;
-        p.w.derived[2][c] = -0.5 * cs * inv_d;
-        p.w.derived[3][c] = pr * p.inv_gm1 + d * ke;
-        p.w.derived[4][c] = ke;
-        p.w.derived[5][c] = inv_d;
         int i, j, k;
         decode(p.g, c, i, j, k);
-        bool const in = interior(p.g, i, j, k);
+        double cb[5];
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
-            p.w.weight[f][c] = in ? p.wscale * p.cbar.f[f][c] : 0.0;
+            cb[f] = p.cbar.f[f][c];
         }
+        prep_cell(p, p.prim, p.wscale, cb, c, i, j, k);
     }
 }
 
@@ -155,7 +170,8 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
                 if (any) {
                     FaceSide const L = load_side(p, c, a);
                     FaceSide const R = load_side(p, cr, a);
-                    hllc_bar(L, R, dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], p.ds[a], p.inv_gm1, bL, bR);
+                    hllc_bar(L, R, dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], p.ds[a], p.hds[a], p.inv_gm1,
+                             bL, bR);
                 }
             }
             self[0] += bL.r;
@@ -177,7 +193,10 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
     }
 }
 
-__global__ void __launch_bounds__(kThreads) adj_gather_kernel(AdjParams p)
+// With prev.f[0] set (mode kAdjStep), the same pass also does the prep of the
+// reverse step that follows -- the state one step earlier, `prev`, with
+// weight scale wscale_prev -- from the cotangent it has just formed.
+__global__ void __launch_bounds__(kThreads) adj_gather_kernel(AdjParams p, CBundle<double> prev, double wscale_prev)
 {
     long long const n = p.g.ncell();
     long long const stride[3] = {1, p.g.s1, p.g.s2};
@@ -206,11 +225,19 @@ __global__ void __launch_bounds__(kThreads) adj_gather_kernel(AdjParams p)
             double const gp = pb[1] * p.gm1;
             double const c0 = p.cbar.f[0][c], c1 = p.cbar.f[1][c];
             double const c2 = p.cbar.f[2][c], c3 = p.cbar.f[3][c], c4 = p.cbar.f[4][c];
-            p.out.f[0][c] = c0 + pb[0] + gp * ke - inv_d * (pb[2] * u0 + pb[3] * u1 + pb[4] * u2);
-            p.out.f[1][c] = c1 + gp;
-            p.out.f[2][c] = c2 + pb[2] * inv_d - gp * u0;
-            p.out.f[3][c] = c3 + pb[3] * inv_d - gp * u1;
-            p.out.f[4][c] = c4 + pb[4] * inv_d - gp * u2;
+            double r[5];
+            r[0] = c0 + pb[0] + gp * ke - inv_d * (pb[2] * u0 + pb[3] * u1 + pb[4] * u2);
+            r[1] = c1 + gp;
+            r[2] = c2 + pb[2] * inv_d - gp * u0;
+            r[3] = c3 + pb[3] * inv_d - gp * u1;
+            r[4] = c4 + pb[4] * inv_d - gp * u2;
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                p.out.f[f][c] = r[f];
+            }
+            if (prev.f[0] != nullptr) { // this cell's derived data were read above
+                prep_cell(p, prev, wscale_prev, r, c, idx[0], idx[1], idx[2]);
+            }
         } else if (p.mode == kAdjInitial) {
             // prim_to_cons: e = p/(gamma-1) + d |u|^2 / 2, m = d u
             double const c0 = p.cbar.f[0][c], c1 = p.cbar.f[1][c];
@@ -308,9 +335,10 @@ AdjWork adjoint_workspace(void* base, long long ncell)
     return w;
 }
 
-cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> out, int mode, Geom g,
-                                double gamma, double dx0, double dx1, double dx2, double dt, AdjWork const& w, int sms,
-                                cudaStream_t s)
+namespace {
+
+AdjParams make_params(CBundle<double> prim, CBundle<double> cbar, Bundle<double> out, int mode, Geom g, double gamma,
+                      double dx0, double dx1, double dx2, double dt, AdjWork const& w)
 {
     AdjParams p;
     p.g = g;
@@ -324,12 +352,33 @@ cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bund
     p.ds[0] = dx1 * dx2; // uniform_mesh.hpp:33-46
     p.ds[1] = dx2 * dx0;
     p.ds[2] = dx0 * dx1;
+    for (int a = 0; a < 3; ++a) {
+        p.hds[a] = 0.5 * p.ds[a];
+    }
     p.wscale = dt / (dx0 * dx1 * dx2);
     p.mode = mode;
+    return p;
+}
+
+} // namespace
+
+cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> out, int mode, Geom g,
+                                double gamma, double dx0, double dx1, double dx2, double dt, AdjWork const& w, int sms,
+                                cudaStream_t s, bool prepared, CBundle<double> const* prev, double dt_prev)
+{
+    AdjParams const p = make_params(prim, cbar, out, mode, g, gamma, dx0, dx1, dx2, dt, w);
     long long const n = g.ncell();
-    adj_prep_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    if (!prepared) {
+        adj_prep_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    }
     adj_face_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
-    adj_gather_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    CBundle<double> pv{};
+    double ws_prev = 0.0;
+    if (prev != nullptr && mode == kAdjStep) {
+        pv = *prev;
+        ws_prev = dt_prev / (dx0 * dx1 * dx2);
+    }
+    adj_gather_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p, pv, ws_prev);
     return cudaGetLastError();
 }
 

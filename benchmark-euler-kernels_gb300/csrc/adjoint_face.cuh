@@ -7,6 +7,8 @@
 // the derivative is the mean of the two one-sided derivatives.
 #pragma once
 
+#include <cstring>
+
 #if defined(__CUDACC__)
 #define EULR_ADJ_FN __host__ __device__ __forceinline__
 #else
@@ -23,6 +25,44 @@ EULR_ADJ_FN double adj_rcp(double x)
 #else
     return 1.0 / x;
 #endif
+}
+
+// Decisions on the integer pipe: on GB300 an FP64 compare takes a full slot
+// of the FP64 pipe, which bounds the reverse step; the same decisions taken
+// on the bit patterns cost nothing there.
+EULR_ADJ_FN long long adj_bits(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return __double_as_longlong(x);
+#else
+    long long b;
+    std::memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+
+// Integer key with the order of the doubles, -0 and +0 equal (ties must
+// see them as one value).
+EULR_ADJ_FN long long adj_key(double x)
+{
+    long long const b = adj_bits(x);
+    return (b << 1) == 0 ? 0 : (b ^ ((b >> 63) & 0x7fffffffffffffffLL));
+}
+
+EULR_ADJ_FN bool adj_neg(double x) // x < 0
+{
+    long long const b = adj_bits(x);
+    return b < 0 && (b << 1) != 0;
+}
+
+EULR_ADJ_FN bool adj_pos(double x) // x > 0 (for non-NaN x)
+{
+    return adj_bits(x) > 0;
+}
+
+EULR_ADJ_FN bool adj_zero(double x) // x == +0 or -0
+{
+    return (adj_bits(x) << 1) == 0;
 }
 
 // One side of a face in the face frame: normal velocity un, tangential t1, t2.
@@ -87,16 +127,18 @@ EULR_ADJ_FN double tie_branch_bar(FaceSide const& q, double a, double iS, double
 
 // Transposed HLLC flux of one face (hllc.hpp:50-105).  The cotangent of the
 // face flux is ds * (dd, de, dn, dt1, dt2) in the face frame (mass, energy,
-// normal and tangential momentum); adds the cotangents of both sides'
-// primitive states to bL and bR.
+// normal and tangential momentum; hds = ds / 2); adds the cotangents of both
+// sides' primitive states to bL and bR.
 EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, double de, double dn, double dt1,
-                          double dt2, double ds, double inv_gm1, FaceBar& bL, FaceBar& bR)
+                          double dt2, double ds, double hds, double inv_gm1, FaceBar& bL, FaceBar& bR)
 {
     // S_L = min(un_L, un_R) - max(c_L, c_R), S_R = max(un_L, un_R) + max(c_L, c_R)
-    bool const u_lt = L.un < R.un;
-    bool const u_gt = R.un < L.un;
-    bool const c_lt = L.c < R.c;
-    bool const c_gt = R.c < L.c;
+    long long const kuL = adj_key(L.un), kuR = adj_key(R.un);
+    long long const kcL = adj_key(L.c), kcR = adj_key(R.c);
+    bool const u_lt = kuL < kuR;
+    bool const u_gt = kuR < kuL;
+    bool const c_lt = kcL < kcR;
+    bool const c_gt = kcR < kcL;
     double const umin = u_gt ? R.un : L.un;
     double const umax = u_lt ? R.un : L.un;
     double const cmax = c_lt ? R.c : L.c;
@@ -108,13 +150,13 @@ EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, doubl
     double const rcR = R.r * aR;
     double const num = (R.p - L.p) + rcL * L.un - rcR * R.un;
     double const den = rcL - rcR; // rcL <= 0 <= rcR: den < 0, so ustar > 0 exactly when num < 0
-    bool const left = num < 0.0;
-    bool const tie = num == 0.0;
+    bool const left = adj_neg(num);
+    bool const tie = adj_zero(num);
     // at a tie each of the two branches takes half of the cotangent
-    double const sc = tie ? 0.5 * ds : ds;
+    double const sc = tie ? hds : ds;
     double const gd = sc * dd, ge = sc * de, gn = sc * dn, gt1 = sc * dt1, gt2 = sc * dt2;
 
-    if (SL > 0.0 || SR < 0.0) {
+    if (adj_pos(SL) || adj_neg(SR)) {
         // S_L * S_R > 0: the flux is the upwind side's physical flux (ustar > 0 picks L)
         FaceSide const& q = left ? L : R;
         FaceBar& bq = left ? bL : bR;

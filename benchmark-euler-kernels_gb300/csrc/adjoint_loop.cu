@@ -355,15 +355,21 @@ int eulr_adjoint_backward(eulr_adjoint* a, eulr_prim_cf64 prim_final_bar, eulr_p
             ADJ_CUDA(launch_cons_to_prim_adjoint(cb(pN), cb(pT), bb(cbar), 0, a->ncell, a->gamma, a->sms, a->stream),
                      "cons_to_prim adjoint");
         }
+        // each gather pass also prepares the next reverse step of the segment
         for (int n = s1 - 1; n >= s0; --n) {
             double* pn[5];
+            double* pp[5];
             for (int f = 0; f < 5; ++f) {
                 pn[f] = a->seg(n - s0, f);
+                pp[f] = n - 1 >= s0 ? a->seg(n - 1 - s0, f) : nullptr;
             }
             int const mode = n == 0 ? kAdjInitial : kAdjStep;
+            CBundle<double> const prev = cb(pp);
+            bool const fuse = mode == kAdjStep && n - 1 >= s0;
             ADJ_CUDA(launch_step_adjoint(cb(pn), cb(cbar), bb(mode == kAdjStep ? cbar : p0), mode, g, a->gamma,
                                          a->dx[0], a->dx[1], a->dx[2], a->dts[static_cast<size_t>(n)], w, a->sms,
-                                         a->stream),
+                                         a->stream, n < s1 - 1, fuse ? &prev : nullptr,
+                                         fuse ? a->dts[static_cast<size_t>(n - 1)] : 0.0),
                      "reverse step");
         }
         ADJ_CUDA(cudaEventRecord(rev.b, a->stream), "cudaEventRecord");

@@ -159,9 +159,14 @@ struct AdjWork {
 
 size_t adjoint_workspace_bytes(long long ncell);
 AdjWork adjoint_workspace(void* base, long long ncell);
+// One reverse step.  prepared: the workspace already holds this step's prep
+// (a previous call's fused prep).  prev (mode kAdjStep): also prepare the
+// next reverse step -- the state one step earlier, stepped with dt_prev -- in
+// the gather pass.
 cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> out, int mode, Geom g,
                                 double gamma, double dx0, double dx1, double dx2, double dt, AdjWork const& w, int sms,
-                                cudaStream_t s);
+                                cudaStream_t s, bool prepared = false, CBundle<double> const* prev = nullptr,
+                                double dt_prev = 0.0);
 cudaError_t launch_cons_to_prim_adjoint(CBundle<double> prim, CBundle<double> pbar, Bundle<double> cbar,
                                         int accumulate, long long n, double gamma, int sms, cudaStream_t s);
 cudaError_t launch_prim_to_cons_adjoint(CBundle<double> prim, CBundle<double> cbar, Bundle<double> pbar,

@@ -77,7 +77,8 @@ extern "C" void host_godunov_adjoint(const double* const* prim, const double* co
             FaceBar bL, bR;
             zero(bL);
             zero(bR);
-            hllc_bar(side(c, a), side(cr, a), dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], ds[a], inv_gm1, bL, bR);
+            hllc_bar(side(c, a), side(cr, a), dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], ds[a], 0.5 * ds[a],
+                     inv_gm1, bL, bR);
             double const lv[5] = {bL.r, bL.p, bL.un, bL.t1, bL.t2};
             double const rv[5] = {bR.r, bR.p, bR.un, bR.t1, bR.t2};
             int const map[5] = {0, 1, 2 + a, 2 + b, 2 + e};
