@@ -162,3 +162,23 @@ def test_async_state_read_and_fused_load(cuda, euler, oracle_lib):
         sim.set_prim(host)
         with pytest.raises(euler.EulerError):
             sim.get_state(prim=torch.empty((5, 16, 18, 20), dtype=torch.float64), wait=False)
+
+
+@pytest.mark.parametrize("precision", ["f32c", "f32", "f32c_hilo"])
+def test_fp32_tiny_and_ragged_grids(cuda, euler, oracle_lib, precision):
+    """The FP32 engines on grids with one interior cell, none, a single partial
+    tile (35 x 3 x 3: one row of 33 cells over a 32-wide tile) and long thin
+    columns, against the FP64 oracle loop."""
+    O = oracle_lib
+    for shape in ((3, 3, 3), (2, 5, 4), (35, 3, 3), (4, 4, 70), (37, 12, 5)):
+        prim0 = O.random_prim(*shape, seed=9)
+        p = prim0.copy()
+        c = O.prim_to_cons(p, 1.4)
+        dx = (0.1, 0.1, 0.1)
+        O.simulate(p, c, 1.4, dx, 0.4, 3)
+        with euler.Simulation(*shape, 1.4, dx, 0.4, precision=precision) as sim:
+            sim.set_prim(prim0)
+            sim.advance(3)
+            _, cg = sim.state_numpy()
+            assert sim.status() == 0
+        assert max(rel_linf(cg, c)) <= 2e-5, (precision, shape, rel_linf(cg, c))
