@@ -280,8 +280,11 @@ template <class T>
 int enqueue_step_t(eulr_batch* b, int dir)
 {
     int const n = static_cast<int>(b->grids.size());
-    B_CUDA(launch_ghost_batch<T>(static_cast<GhostParams<T> const*>(b->d_ghost[dir]), n, b->ghost_blocks, b->stream),
-           "batch ghost launch");
+    if (is_f64(b)) { // FP32 states: ghost layers set once at load (prepare_grid)
+        B_CUDA(launch_ghost_batch<T>(static_cast<GhostParams<T> const*>(b->d_ghost[dir]), n, b->ghost_blocks,
+                                     b->stream),
+               "batch ghost launch");
+    }
     BatchParams<T> bp{};
     bp.grids = static_cast<FluxParams<T> const*>(b->d_params[dir]);
     bp.items = b->d_items;
@@ -324,6 +327,24 @@ int prepare_grid(eulr_batch* b, int g)
                                      b->comp != kCompNone ? 1 : 0, &b->sc[g].wmax, b->sms, b->stream),
                "invdt");
         B_CUDA(launch_finalize_dt<float>(&b->sc[g], static_cast<float>(b->cfl), 0, b->stream), "finalize");
+        // the ghost layer never changes: copy 1 gets copy 0's ghost cons once, and its
+        // max invdt is kept for every later step
+        GhostParams<float> q{};
+        q.g = G.g;
+        q.cons_in = cbundle_of<float>(G.cons[0]);
+        q.cons_out = bundle_of<float>(G.cons[1]);
+        if (b->comp == kCompHiLo) {
+            q.lo_in = cbundle_of<float>(G.lo[0]);
+            q.lo_out = bundle_of<float>(G.lo[1]);
+        }
+        q.comp = b->comp;
+        q.gamma = gm;
+        q.gm1 = gm - 1.0f;
+        q.invdx0 = 1.0f / static_cast<float>(G.dx[0]);
+        q.invdx1 = 1.0f / static_cast<float>(G.dx[1]);
+        q.invdx2 = 1.0f / static_cast<float>(G.dx[2]);
+        q.wmax = &b->sc[g].ghost_wmax;
+        B_CUDA(launch_ghost_shell<float>(q, b->sms, b->stream), "ghost shell");
     }
     G.loaded = true;
     return EULR_SUCCESS;

@@ -686,9 +686,11 @@ __device__ __forceinline__ void ghost_shell_body(GhostParams<T> const& p)
         } else if (c < 2 * plane) {
             o = (c < plane) ? c : c - plane + plane * (g.n2 - 1);
         } else {
-            long long const r0 = c - 2 * plane;
-            int const k = 1 + static_cast<int>(r0 / ring);
-            int const r = static_cast<int>(r0 % ring);
+            // grids hold < 2^31 cells: the ring index fits 32-bit division
+            unsigned const r0 = static_cast<unsigned>(c - 2 * plane);
+            unsigned const q = r0 / static_cast<unsigned>(ring);
+            int const k = 1 + static_cast<int>(q);
+            int const r = static_cast<int>(r0 - q * static_cast<unsigned>(ring));
             int i, j;
             if (r < g.n0) {
                 i = r;
@@ -711,7 +713,7 @@ __device__ __forceinline__ void ghost_shell_body(GhostParams<T> const& p)
         T pr, u0, u1, u2;
         if (p.prim_out.f[0] == nullptr) {
             // cons-only FP32 state: only the cons words and the wavespeed
-            T const r = T(1) / d;
+            T const r = rcp_rn(d); // = 1/d correctly rounded
             u0 = m0 * r;
             u1 = m1 * r;
             u2 = m2 * r;
@@ -739,7 +741,14 @@ __device__ __forceinline__ void ghost_shell_body(GhostParams<T> const& p)
             p.prim_out.f[4][o] = u2;
             p.cs_out[o] = sqrt_rn(div_rn(mul_rn(p.gamma, pr), d));
         }
-        T const v = cell_invdt_exact(d, pr, u0, u1, u2, p.gamma, p.invdx0, p.invdx1, p.invdx2);
+        T v;
+        if (p.prim_out.f[0] == nullptr) {
+            // FP32 states: the sound speed as their step kernel forms it
+            T const cs = fast_sound_speed((p.gamma * rcp_rn(d)) * pr);
+            v = (cs + abs_(u0)) * p.invdx0 + (cs + abs_(u1)) * p.invdx1 + (cs + abs_(u2)) * p.invdx2;
+        } else {
+            v = cell_invdt_exact(d, pr, u0, u1, u2, p.gamma, p.invdx0, p.invdx1, p.invdx2);
+        }
         wmax = (v > wmax) ? v : wmax;
     }
     __shared__ T warp_best[8];
@@ -786,7 +795,8 @@ __device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time,
         s->t = __dadd_rn(s->t, step);
         s->steps += 1;
     }
-    T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(s->wmax)));
+    unsigned long long const wk = s->wmax > s->ghost_wmax ? s->wmax : s->ghost_wmax;
+    T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(wk)));
     T const dt = (m > T(0)) ? rcp_rn(m) : (sizeof(T) == 8 ? T(DBL_MAX) : T(FLT_MAX));
     s->dt = static_cast<double>(dt);
     s->wmax = 0ull;

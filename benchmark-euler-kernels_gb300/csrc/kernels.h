@@ -27,6 +27,7 @@ struct SimScalars {
     long long steps;         // steps taken
     int status;              // bit 0: a cell became non-finite or non-physical
     int pad;
+    unsigned long long ghost_wmax; // FP32 states: max invdt of the ghost layer, which never changes (set at load)
 };
 
 // TMA descriptors of the seven staged fields (d, p, u0, u1, u2, c, e) of the

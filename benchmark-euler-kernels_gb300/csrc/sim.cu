@@ -205,21 +205,17 @@ void setup_tma(eulr_sim* s)
 
 // One fused step from copy `in` to copy `1-in`; with `ev` (4 events) the
 // launches are bracketed for per-kernel timing.
+// The ghost layer of copy `in` carried to copy `out` (cons, low words, and
+// for FP64 prim and sound speed), its max invdt into *wmax.
 template <class T>
-int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
+GhostParams<T> ghost_params(eulr_sim* s, int in, int out, unsigned long long* wmax)
 {
-    int const out = 1 - in;
-    T const ix0 = T(1) / static_cast<T>(s->dx[0]);
-    T const ix1 = T(1) / static_cast<T>(s->dx[1]);
-    T const ix2 = T(1) / static_cast<T>(s->dx[2]);
     T const gamma = static_cast<T>(s->gamma);
-    bool const has_lo = s->comp == kCompHiLo;
-
     GhostParams<T> gp{};
     gp.g = s->g;
     gp.cons_in = cbundle_of<T>(s->cons[in]);
     gp.cons_out = bundle_of<T>(s->cons[out]);
-    if (has_lo) {
+    if (s->comp == kCompHiLo) {
         gp.lo_in = cbundle_of<T>(s->lo[in]);
         gp.lo_out = bundle_of<T>(s->lo[out]);
     }
@@ -230,14 +226,35 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
     gp.comp = s->comp;
     gp.gamma = gamma;
     gp.gm1 = gamma - T(1);
-    gp.invdx0 = ix0;
-    gp.invdx1 = ix1;
-    gp.invdx2 = ix2;
-    gp.wmax = &s->sc->wmax;
+    gp.invdx0 = T(1) / static_cast<T>(s->dx[0]);
+    gp.invdx1 = T(1) / static_cast<T>(s->dx[1]);
+    gp.invdx2 = T(1) / static_cast<T>(s->dx[2]);
+    gp.wmax = wmax;
+    return gp;
+}
+
+// One fused step from copy `in` to copy `1-in`; with `ev` (4 events) the
+// launches are bracketed for per-kernel timing.  The ghost layer is rebuilt
+// every step for the FP64 state (the reference runs cons_to_prim over ghosts,
+// and the first step's ghost prim is the loaded one); the FP32 states' ghost
+// cons never change, so both copies get them once at load and the step
+// skips the ghost launch (its wavespeed is the stored ghost_wmax).
+template <class T>
+int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
+{
+    int const out = 1 - in;
+    T const ix0 = T(1) / static_cast<T>(s->dx[0]);
+    T const ix1 = T(1) / static_cast<T>(s->dx[1]);
+    T const ix2 = T(1) / static_cast<T>(s->dx[2]);
+    T const gamma = static_cast<T>(s->gamma);
+    bool const has_lo = s->comp == kCompHiLo;
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[0], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_ghost_shell<T>(gp, s->sms, s->stream), "ghost shell launch");
+    if (is_f64(s)) {
+        SIM_CUDA(launch_ghost_shell<T>(ghost_params<T>(s, in, out, &s->sc->wmax), s->sms, s->stream),
+                 "ghost shell launch");
+    }
 
     FluxParams<T> p{};
     p.g = s->g;
@@ -318,6 +335,9 @@ int prepare_loaded(eulr_sim* s, bool derive_cons = false)
                                        s->comp != kCompNone ? 1 : 0, &s->sc->wmax, s->sms, s->stream),
                  "invdt launch");
         SIM_CUDA(launch_finalize_dt<float>(s->sc, static_cast<float>(s->cfl), 0, s->stream), "finalize launch");
+        // the ghost layer, once for every later step: copy 1 gets copy 0's ghost cons
+        SIM_CUDA(launch_ghost_shell<float>(ghost_params<float>(s, 0, 1, &s->sc->ghost_wmax), s->sms, s->stream),
+                 "ghost shell launch");
     }
     s->loaded = true;
     return EULR_SUCCESS;
@@ -811,8 +831,7 @@ int eulr_sim_set_dt_sequence(eulr_sim* s, const double* dts, long long n)
 
 int eulr_sim_launches_per_step(eulr_sim* s)
 {
-    (void)s;
-    return 3;
+    return (s != nullptr && !is_f64(s)) ? 2 : 3;
 }
 
 int eulr_sim_profile_step(eulr_sim* s, float ms[3])
