@@ -182,3 +182,47 @@ def test_fp32_tiny_and_ragged_grids(cuda, euler, oracle_lib, precision):
             _, cg = sim.state_numpy()
             assert sim.status() == 0
         assert max(rel_linf(cg, c)) <= 2e-5, (precision, shape, rel_linf(cg, c))
+
+
+def test_objects_release_their_memory_and_report_oom(cuda, euler):
+    """Creating and destroying simulations, batches and adjoints leaves the
+    device's free memory where it was; a state larger than the device is an
+    out-of-memory status, not a crash."""
+    torch = cuda
+    free0 = None
+    for it in range(6):
+        if it == 1:  # after one round: kernels loaded, per-device scratch allocated
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            free0, _ = torch.cuda.mem_get_info()
+        with euler.Simulation(66, 66, 66, precision="f64") as s:
+            s.init_implode()
+            s.advance(2)
+        with euler.Simulation(66, 66, 66, precision="f32c") as s:
+            s.init_implode()
+            s.advance(2)
+        with euler.Batch([(34, 26, 18, 1.4, 0.1, 0.1, 0.1)] * 3, precision="f32c") as b:
+            for g in range(3):
+                b.init_step(g, 0.3, 0.5, 0.5)
+            b.advance(2)
+        a = euler.Adjoint(18, 18, 18, 4, checkpoint_every=2)
+        p = torch.ones((5, 18, 18, 18), dtype=torch.float64, device="cuda")
+        p[2:] = 0.0
+        a.forward(p)
+        g0 = torch.empty_like(p)
+        a.backward(torch.zeros_like(p), g0)
+        a.close()
+        del p, g0
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free1, _ = torch.cuda.mem_get_info()
+    assert abs(free1 - free0) < 8 << 20, (free0, free1)
+    # 1200^3 cells x 22 FP64 fields is ~300 GB, beyond one GB300
+    with pytest.raises(euler.EulerError) as err:
+        euler.Simulation(1200, 1200, 1200)
+    assert err.value.status == -5  # EULR_ERR_OUT_OF_MEMORY
+    # the library keeps working afterwards
+    with euler.Simulation(18, 18, 18) as s:
+        s.init_implode()
+        s.advance(1)
+        assert s.status() == 0
