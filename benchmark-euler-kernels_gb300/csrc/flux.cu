@@ -30,6 +30,7 @@
 // copies still in flight and ends the CTA.
 #include "euler_device.cuh"
 #include "kernels.h"
+#include "step_common.cuh"
 
 #include <cfloat>
 
@@ -37,9 +38,7 @@ namespace eulr {
 
 namespace {
 
-constexpr int kFields = 7;          // d, p, u0, u1, u2, c, e
 constexpr int kWaitTries = 1 << 20; // mbarrier.try_wait attempts before giving up
-constexpr long long kInfBits = 0x7ff0000000000000LL;
 
 template <class T, int TX, int TY, int NSLOT>
 struct TileLayout {
@@ -63,11 +62,6 @@ struct TileLayout {
     static constexpr size_t BYTES = 128 + MBAR_BYTES + sizeof(T) * static_cast<size_t>(ELEMS);
     static constexpr unsigned TX_BYTES = kFields * PLANE * sizeof(T); // bytes one slot's TMA delivers
 };
-
-__device__ __forceinline__ unsigned smem_u32(const void* p)
-{
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
 
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
 {
@@ -116,28 +110,6 @@ __device__ __forceinline__ T* slot_field(T* smem, int slot, int field)
     using L = TileLayout<T, TX, TY, NSLOT>;
     return smem + (slot * kFields + field) * L::PLANE_PAD;
 }
-
-// Pressure of an FP32 conservative state: compensated states rescue the
-// low-pressure cells in FP64 (pressure_f32c), plain FP32 does not.
-template <int COMP>
-__device__ __forceinline__ float cons_pressure(float d, float e, float m0, float m1, float m2, float r, float gm1,
-                                               const float* lo)
-{
-    if (COMP != kCompNone) {
-        return pressure_f32c(d, e, m0, m1, m2, r, gm1, lo);
-    }
-    return gm1 * (e - (0.5f * r) * (m0 * m0 + m1 * m1 + m2 * m2));
-}
-template <int COMP>
-__device__ __forceinline__ double cons_pressure(double, double, double, double, double, double, double, const double*)
-{
-    return 0.0;
-}
-
-// Sound speed sqrt(gamma p / rho) = x * rsqrt(x): rsqrt costs fewer FP64
-// instructions than a correctly rounded sqrt; the result is within ~2 ulps.
-__device__ __forceinline__ double fast_sound_speed(double c2) { return c2 * rsqrt(c2); }
-__device__ __forceinline__ float fast_sound_speed(float c2) { return c2 * rsqrtf(c2); }
 
 // Issue the TMA loads of plane k (x origin i0-1, y origin j0-1) into `slot`.
 template <class T, int TX, int TY, int NSLOT>
@@ -232,36 +204,6 @@ __device__ __forceinline__ void store_flux(T* out, int stride, int idx, int dir,
     out[(2 + (dir + 1) % 3) * stride + idx] = f.t1;
     out[(2 + (dir + 2) % 3) * stride + idx] = f.t2;
 }
-
-__device__ __forceinline__ long long wave_key(double v)
-{
-    long long const b = dbits(v);
-    return b <= kInfBits ? b : 0LL; // NaN never wins (the reference skips it)
-}
-__device__ __forceinline__ long long wave_key(float v) { return wave_key(static_cast<double>(v)); }
-
-__device__ __forceinline__ bool cell_ok(double d, double pr, double invdt)
-{
-    return finite_positive(d) && finite_positive(pr) && dbits(invdt) < kInfBits;
-}
-__device__ __forceinline__ bool cell_ok(float d, float pr, float invdt)
-{
-    return d > 0.0f && pr > 0.0f && invdt <= 3.0e38f;
-}
-
-// sum + err += k*f without rounding error in the product (TwoProduct via
-// FMA) or in the running sum (Knuth's TwoSum); the errors collect in err.
-__device__ __forceinline__ void compensated_add(float& sum, float& err, float k, float f)
-{
-    float const prod = k * f;
-    float const prod_err = fmaf(k, f, -prod);
-    float const s = sum + prod;
-    float const bb = s - sum;
-    float const sum_err = (sum - (s - bb)) + (prod - bb);
-    sum = s;
-    err += sum_err + prod_err;
-}
-__device__ __forceinline__ void compensated_add(double&, double&, double, double) {}
 
 // Per-CTA state of the tile engine that lives across work items.
 template <class T>
@@ -564,20 +506,6 @@ __device__ __forceinline__ TileCtx<T> make_ctx(unsigned char* smem_dyn)
     return c;
 }
 
-// dt/dv, from the device dt when there is one (godunov.hpp:37 with the
-// cfl * dt of euler_simulation.cpp:65), evaluated in double.
-template <class T>
-__device__ __forceinline__ T dt_over_dv(FluxParams<T> const& p)
-{
-    if (p.dt_seq != nullptr) {
-        return static_cast<T>(p.dt_seq[*p.step_dev] / p.dv);
-    }
-    if (p.dt_dev != nullptr) {
-        return static_cast<T>((p.cfl * *p.dt_dev) / p.dv);
-    }
-    return p.dtodv;
-}
-
 template <class T, int TX, int TY, int NSLOT, int MODE, bool TMA, int COMP>
 __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant__ FluxParams<T> p,
                                                            const __grid_constant__ TmaMaps maps)
@@ -827,516 +755,6 @@ __global__ void finalize_batch_kernel(SimScalars* s, int ngrids, T cfl, int add_
 constexpr int kTX = 32;
 constexpr int kTY = 8;
 
-// Chunk length (planes per work item) that balances the persistent grid:
-// the step lasts as long as its busiest CTA, while each extra chunk costs
-// one more z face row and two more staged planes (about 1/(3 kchunk) of a
-// chunk's work).  Scores every length from 8 to 64 by
-//   (planes / (resident CTAs x planes of the busiest CTA)) x (1 - 1/(3 kchunk))
-// and keeps the best.
-int choose_kchunk(int columns, int iz, long long slots)
-{
-    int best = 64;
-    double best_score = -1.0;
-    for (int kc = 8; kc <= 64; ++kc) {
-        long long const chunks = (iz + kc - 1) / kc;
-        long long const items = chunks * columns;
-        long long const rounds = (items + slots - 1) / slots; // items of the busiest CTA
-        double const busiest = static_cast<double>(rounds) * kc;
-        double const score = (static_cast<double>(iz) * columns / (static_cast<double>(slots) * busiest)) *
-                             (1.0 - 1.0 / (3.0 * kc));
-        if (score > best_score + 1e-9) {
-            best_score = score;
-            best = kc;
-        }
-    }
-    return best;
-}
-
-// ------------------------------------------------- FP32 step, column engine
-// The fused step of the FP32 states (cons only in HBM) with a regular
-// face-per-thread mapping.  Thread (ti, tj) of a 32 x 8 CTA owns the column
-// (i0 + ti, j0 + tj) and marches it up z, keeping its cell's primitive state
-// of planes k and k+1 in registers.  Per plane it solves
-//   x: the face on its cell's left  (the right one is lane+1's, by shuffle;
-//      lane 31 also solves the tile's right boundary face),
-//   y: the face below its cell      (the one above is the next row's, through
-//      shared memory; row 7 also solves the tile's top boundary faces),
-//   z: the face above its cell      (both sides in registers; the face below
-//      is the previous plane's).
-// Shared memory holds only plane k's primitive tile with its halo ring (for
-// the y and boundary neighbours) and the y fluxes.  Cons of plane k+2 (own
-// cell) and k+1 (halo ring, threads 0..79) are prefetched into registers a
-// plane ahead.
-//
-// Plain (kCompNone) and compensated (kCompSum) FP32 states; the state with
-// stored low words (kCompHiLo) keeps the shared-memory tile engine, whose
-// register budget fits them.  The compensated update sums the cell's six
-// signed face terms into cons without intermediate rounding:
-//   * cubic cells (k0 == k1 == k2): the six fluxes are summed exactly (TwoSum
-//     chain), multiplied by k exactly (TwoProduct), and added to cons by a
-//     TwoSum, then rounded once;
-//   * otherwise, per axis, the flux difference is formed exactly (TwoSum),
-//     multiplied by k_d exactly (TwoProduct) and added by a TwoSum.
-namespace f32col {
-
-constexpr int TX = 32;
-constexpr int TY = 8;
-constexpr int NT = TX * TY;
-constexpr int HX = TX + 2;
-constexpr int HY = TY + 2;
-constexpr int PLANE = HX * HY; // 340
-constexpr int NHALO = 2 * TY + 2 * TX; // 80: left, right columns, bottom, top rows
-
-struct Prim7 {
-    float d, p, u[3], c, e;
-};
-
-struct Raw5 {
-    float d, e, m[3];
-};
-
-__device__ __forceinline__ Side<float> side_of(Prim7 const& q, int dir)
-{
-    Side<float> s;
-    s.d = q.d;
-    s.p = q.p;
-    s.un = q.u[dir];
-    s.ut1 = q.u[(dir + 1) % 3];
-    s.ut2 = q.u[(dir + 2) % 3];
-    s.c = q.c;
-    s.e = q.e;
-    return s;
-}
-
-// The flux of a face in global components (d, e, m0, m1, m2).
-__device__ __forceinline__ void to_global(Flux<float> const& f, int dir, float* g)
-{
-    g[0] = f.d;
-    g[1] = f.e;
-    g[2 + dir] = f.n;
-    g[2 + (dir + 1) % 3] = f.t1;
-    g[2 + (dir + 2) % 3] = f.t2;
-}
-
-template <int COMP>
-__device__ __forceinline__ Prim7 prim_of(Raw5 const& r, FluxParams<float> const& p)
-{
-    Prim7 q;
-    float const ir = rcp_rn(r.d);
-    q.d = r.d;
-    q.e = r.e;
-    q.u[0] = r.m[0] * ir;
-    q.u[1] = r.m[1] * ir;
-    q.u[2] = r.m[2] * ir;
-    q.p = cons_pressure<COMP>(r.d, r.e, r.m[0], r.m[1], r.m[2], ir, p.gm1, nullptr);
-    q.c = fast_sound_speed(p.gamma * q.p * ir);
-    return q;
-}
-
-// A benign state for cells outside the array (no face touching one is used).
-__device__ __forceinline__ Raw5 outside() { return Raw5{1.0f, 2.5f, {0.0f, 0.0f, 0.0f}}; }
-
-__device__ __forceinline__ Raw5 load_raw(FluxParams<float> const& p, int i, int j, int k)
-{
-    if (i >= p.g.n0 || j >= p.g.n1) {
-        return outside();
-    }
-    long long const o = p.g.at(i, j, k);
-    Raw5 r;
-    r.d = __ldg(p.cons_in.f[0] + o);
-    r.e = __ldg(p.cons_in.f[1] + o);
-    r.m[0] = __ldg(p.cons_in.f[2] + o);
-    r.m[1] = __ldg(p.cons_in.f[3] + o);
-    r.m[2] = __ldg(p.cons_in.f[4] + o);
-    return r;
-}
-
-// Asynchronous 4-byte global->shared copies (cp.async): the prefetched cons
-// of the next planes wait in shared memory instead of registers.
-__device__ __forceinline__ void cp_async4(float* dst, const float* src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// Starts copying the cons of cell (i, j, k) to dst[f * stride] (benign values for cells outside the array).
-__device__ __forceinline__ void prefetch_raw(float* dst, int stride, FluxParams<float> const& p, int i, int j, int k)
-{
-    if (i >= p.g.n0 || j >= p.g.n1) {
-        Raw5 const b = outside();
-        dst[0] = b.d;
-        dst[stride] = b.e;
-        dst[2 * stride] = b.m[0];
-        dst[3 * stride] = b.m[1];
-        dst[4 * stride] = b.m[2];
-        return;
-    }
-    long long const o = p.g.at(i, j, k);
-#pragma unroll
-    for (int f = 0; f < 5; ++f) {
-        cp_async4(dst + f * stride, p.cons_in.f[f] + o);
-    }
-}
-
-__device__ __forceinline__ Raw5 read_raw(float const* src, int stride)
-{
-    return Raw5{src[0], src[stride], {src[2 * stride], src[3 * stride], src[4 * stride]}};
-}
-
-__device__ __forceinline__ void halo_cell(int h, int& hx, int& hy)
-{
-    if (h < TY) {
-        hx = 0;
-        hy = 1 + h;
-    } else if (h < 2 * TY) {
-        hx = HX - 1;
-        hy = 1 + h - TY;
-    } else if (h < 2 * TY + TX) {
-        hx = 1 + h - 2 * TY;
-        hy = 0;
-    } else {
-        hx = 1 + h - 2 * TY - TX;
-        hy = HY - 1;
-    }
-}
-
-__device__ __forceinline__ void put(float* q, int idx, Prim7 const& v)
-{
-    q[0 * PLANE + idx] = v.d;
-    q[1 * PLANE + idx] = v.p;
-    q[2 * PLANE + idx] = v.u[0];
-    q[3 * PLANE + idx] = v.u[1];
-    q[4 * PLANE + idx] = v.u[2];
-    q[5 * PLANE + idx] = v.c;
-    q[6 * PLANE + idx] = v.e;
-}
-
-__device__ __forceinline__ Prim7 get(float const* q, int idx)
-{
-    Prim7 v;
-    v.d = q[0 * PLANE + idx];
-    v.p = q[1 * PLANE + idx];
-    v.u[0] = q[2 * PLANE + idx];
-    v.u[1] = q[3 * PLANE + idx];
-    v.u[2] = q[4 * PLANE + idx];
-    v.c = q[5 * PLANE + idx];
-    v.e = q[6 * PLANE + idx];
-    return v;
-}
-
-// (s, e) += t exactly: s + t = s' + err (Knuth's TwoSum), err collected in e.
-__device__ __forceinline__ void two_sum_into(float& s, float& e, float t)
-{
-    float const n = s + t;
-    float const bb = n - s;
-    e += (s - (n - bb)) + (t - bb);
-    s = n;
-}
-
-struct ColShared {
-    float slot[2][kFields * PLANE];
-    float yflux[5][NT];
-    float raw_own[5 * NT];     // own column, two planes ahead
-    float raw_halo[5 * NHALO]; // halo ring, one plane ahead
-    long long warp_best[NT / 32];
-    int any_bad;
-};
-
-// One work item: interior planes [kb, ke) of the 32 x 8 column tile (tx, ty),
-// kb = 1 + kc * kchunk, with update coefficients k0..k2 (all equal when UNIFORM).
-// Accumulates this thread's max wavespeed and non-physical flag.
-template <int COMP, bool UNIFORM>
-__device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, float k1, float k2, int tx, int ty,
-                                         int kc, ColShared& sh, float& wmaxf, bool& bad)
-{
-    int const tid = threadIdx.x;
-    int const ti = tid % TX; // == lane
-    int const tj = tid / TX; // == warp
-    int const own_idx = (tj + 1) * HX + ti + 1;
-    int hhx = 0, hhy = 0;
-    if (tid < NHALO) {
-        halo_cell(tid, hhx, hhy);
-    }
-    int const i0 = 1 + tx * TX;
-    int const j0 = 1 + ty * TY;
-    int const kb = 1 + kc * p.kchunk;
-    int const ke = min(kb + p.kchunk, p.g.n2 - 1);
-    int const i = i0 + ti;
-    int const j = j0 + tj;
-    bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
-
-    // prologue: planes kb-1 (z face below), kb, kb+1 of the own column,
-    // plane kb of the halo ring
-    if (tid < NHALO) {
-        prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
-    }
-    Raw5 const rb = load_raw(p, i, j, kb - 1);
-    Raw5 rk = load_raw(p, i, j, kb);
-    Raw5 rn = load_raw(p, i, j, kb + 1); // kb + 1 <= ke <= n2 - 1
-    Prim7 q0 = prim_of<COMP>(rk, p);
-    Prim7 q1 = prim_of<COMP>(rn, p);
-    float zlo[5];
-    to_global(hllc_flux(side_of(prim_of<COMP>(rb, p), 2), side_of(q0, 2)), 2, zlo);
-    long long o = p.g.at(min(i, p.g.n0 - 1), min(j, p.g.n1 - 1), kb);
-
-    for (int k = kb; k < ke; ++k) {
-        float* const q = sh.slot[(k - kb) & 1];
-        // stage plane k: the own cell and the halo ring
-        put(q, own_idx, q0);
-        if (tid < NHALO) {
-            cp_async_wait_all(); // this thread's copies of the halo cell (plane k) landed
-            put(q, hhy * HX + hhx, prim_of<COMP>(read_raw(sh.raw_halo + tid, NHALO), p));
-            if (k + 1 < ke) {
-                prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 1);
-            }
-        }
-        // own column plane k+2, consumed at the end of this plane
-        if (k + 2 <= ke) {
-            prefetch_raw(sh.raw_own + tid, NT, p, i, j, k + 2);
-        }
-        __syncthreads(); // plane k staged
-
-        // ---- faces
-        float fxl[5], fyb[5], fzh[5], fxr[5], fyt[5];
-        {
-            float t[5];
-            to_global(hllc_flux(side_of(get(q, own_idx - HX), 1), side_of(q0, 1)), 1, t);
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                sh.yflux[f][tid] = t[f]; // read back after the barrier (registers are scarce here)
-            }
-        }
-        to_global(hllc_flux(side_of(get(q, own_idx - 1), 0), side_of(q0, 0)), 0, fxl);
-        to_global(hllc_flux(side_of(q0, 2), side_of(q1, 2)), 2, fzh);
-#pragma unroll
-        for (int f = 0; f < 5; ++f) {
-            fxr[f] = __shfl_down_sync(0xffffffffu, fxl[f], 1);
-        }
-        if (ti == TX - 1) { // the tile's right boundary face
-            to_global(hllc_flux(side_of(q0, 0), side_of(get(q, own_idx + 1), 0)), 0, fxr);
-        }
-        if (tj == TY - 1) { // the tile's top boundary faces
-            to_global(hllc_flux(side_of(q0, 1), side_of(get(q, own_idx + HX), 1)), 1, fyt);
-        }
-        __syncthreads(); // y fluxes written
-#pragma unroll
-        for (int f = 0; f < 5; ++f) {
-            fyb[f] = sh.yflux[f][tid];
-            if (tj < TY - 1) {
-                fyt[f] = sh.yflux[f][tid + TX];
-            }
-        }
-
-        // ---- update of the own cell
-        if (own) {
-            float u[5] = {rk.d, rk.e, rk.m[0], rk.m[1], rk.m[2]};
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                if (COMP == kCompNone) {
-                    u[f] = u[f] - k0 * (fxr[f] - fxl[f]) - k1 * (fyt[f] - fyb[f]) - k2 * (fzh[f] - zlo[f]);
-                } else if (UNIFORM) {
-                    // sum of the six signed fluxes, exactly, then k times it, exactly
-                    float S = fxl[f];
-                    float eS = 0.0f;
-                    two_sum_into(S, eS, -fxr[f]);
-                    two_sum_into(S, eS, fyb[f]);
-                    two_sum_into(S, eS, -fyt[f]);
-                    two_sum_into(S, eS, zlo[f]);
-                    two_sum_into(S, eS, -fzh[f]);
-                    float const P = k0 * S;
-                    float const eP = fmaf(k0, eS, fmaf(k0, S, -P));
-                    float sum = u[f];
-                    float err = eP;
-                    two_sum_into(sum, err, P);
-                    u[f] = sum + err;
-                } else {
-                    // per axis: the flux difference exactly (TwoSum), times k_d exactly
-                    // (TwoProduct), into the running sum (TwoSum)
-                    float sum = u[f];
-                    float err = 0.0f;
-                    float const kd[3] = {k0, k1, k2};
-                    float const lo_face[3] = {fxl[f], fyb[f], zlo[f]};
-                    float const hi_face[3] = {fxr[f], fyt[f], fzh[f]};
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        float a = lo_face[d];
-                        float ea = 0.0f;
-                        two_sum_into(a, ea, -hi_face[d]);
-                        float const P = kd[d] * a;
-                        err += fmaf(kd[d], ea, fmaf(kd[d], a, -P));
-                        two_sum_into(sum, err, P);
-                    }
-                    u[f] = sum + err;
-                }
-            }
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                p.cons_out.f[f][o] = u[f];
-            }
-            // next step's CFL wavespeed of the new state (time_step.hpp:28-33)
-            float const r = rcp_rn(u[0]);
-            float const v0 = u[2] * r, v1 = u[3] * r, v2 = u[4] * r;
-            float const pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1, nullptr);
-            float const cs = fast_sound_speed((p.gamma * r) * pr);
-            float const invdt = (cs + fabsf(v0)) * p.invdx0 + (cs + fabsf(v1)) * p.invdx1 +
-                                (cs + fabsf(v2)) * p.invdx2;
-            wmaxf = fmaxf(wmaxf, invdt); // NaN never wins
-            bad |= !cell_ok(u[0], pr, invdt);
-        }
-        // march: plane k+1 becomes the current plane
-#pragma unroll
-        for (int f = 0; f < 5; ++f) {
-            zlo[f] = fzh[f];
-        }
-        rk = rn;
-        q0 = q1;
-        if (k + 2 <= ke) {
-            cp_async_wait_all();
-            rn = read_raw(sh.raw_own + tid, NT);
-            q1 = prim_of<COMP>(rn, p);
-        }
-        o += p.g.s2;
-    }
-    __syncthreads(); // the slots are restaged by the next item
-}
-
-// Block max of the threads' wavespeeds into *wmax (ordered bits, one
-// atomicMax per CTA) and the non-physical flag into *status; clears both.
-__device__ __forceinline__ void col_flush(ColShared& sh, float& wmaxf, bool& bad, unsigned long long* wmax,
-                                          int* status)
-{
-    int const tid = threadIdx.x;
-    long long wk = wave_key(wmaxf);
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) {
-        long long const v = __shfl_xor_sync(0xffffffffu, wk, s);
-        wk = v > wk ? v : wk;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        sh.any_bad = 0;
-    }
-    __syncthreads();
-    if (tid % 32 == 0) {
-        sh.warp_best[tid / 32] = wk;
-    }
-    if (bad) {
-        sh.any_bad = 1;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        long long b = sh.warp_best[0];
-#pragma unroll
-        for (int v = 1; v < NT / 32; ++v) {
-            b = sh.warp_best[v] > b ? sh.warp_best[v] : b;
-        }
-        atomicMax(wmax, static_cast<unsigned long long>(b));
-        if (sh.any_bad) {
-            atomicOr(status, 1);
-        }
-    }
-    wmaxf = 0.0f;
-    bad = false;
-}
-
-template <int COMP, bool UNIFORM>
-__global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__ FluxParams<float> p)
-{
-    static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
-    __shared__ __align__(16) ColShared sh;
-    float const dtodv = dt_over_dv(p);
-    float const k0 = dtodv * p.ds0, k1 = dtodv * p.ds1, k2 = dtodv * p.ds2; // UNIFORM: all equal
-    float wmaxf = 0.0f;
-    bool bad = false;
-    int const tiles_xy = p.tiles_x * p.tiles_y;
-    for (int w = blockIdx.x; w < p.nwork; w += gridDim.x) {
-        col_item<COMP, UNIFORM>(p, k0, k1, k2, w % p.tiles_x, (w / p.tiles_x) % p.tiles_y, w / tiles_xy, sh, wmaxf,
-                                bad);
-    }
-    col_flush(sh, wmaxf, bad, p.wmax, p.status);
-}
-
-// The column engine over a batch: CTAs pop (grid, tile x, tile y, chunk)
-// items from the queue, as flux_batch_kernel does; each item's wavespeed goes
-// to its own grid.  Grids with equal face areas take the cubic update.
-template <int COMP>
-__global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant__ BatchParams<float> b)
-{
-    static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
-    static_assert(sizeof(FluxParams<float>) % 4 == 0 && sizeof(FluxParams<float>) / 4 <= NT, "parameter copy");
-    __shared__ __align__(16) ColShared sh;
-    __shared__ __align__(16) FluxParams<float> gp;
-    __shared__ int s_item;
-    int const tid = threadIdx.x;
-    float wmaxf = 0.0f;
-    bool bad = false;
-    for (;;) {
-        __syncthreads(); // everyone is done with the previous item's parameters
-        if (tid == 0) {
-            s_item = static_cast<int>(atomicAdd(b.head, 1u));
-        }
-        __syncthreads();
-        int const item = s_item;
-        if (item >= b.nitems) {
-            break;
-        }
-        int4 const it = b.items[item];
-        if (tid < static_cast<int>(sizeof(FluxParams<float>) / 4)) {
-            reinterpret_cast<int*>(&gp)[tid] = reinterpret_cast<const int*>(&b.grids[it.x])[tid];
-        }
-        __syncthreads();
-        float const dtodv = dt_over_dv(gp);
-        float const k0 = dtodv * gp.ds0, k1 = dtodv * gp.ds1, k2 = dtodv * gp.ds2;
-        if (gp.ds0 == gp.ds1 && gp.ds1 == gp.ds2) {
-            col_item<COMP, true>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
-        } else {
-            col_item<COMP, false>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
-        }
-        col_flush(sh, wmaxf, bad, gp.wmax, gp.status);
-    }
-}
-
-} // namespace f32col
-
-template <int COMP>
-cudaError_t configure_f32col(int* per_sm)
-{
-    int n = 0;
-    cudaError_t const e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_step_kernel<COMP, false>,
-                                                                        f32col::NT, 0);
-    *per_sm = n < 1 ? 1 : n;
-    return e;
-}
-
-template <int COMP>
-cudaError_t launch_f32col(FluxParams<float> p, int sms, cudaStream_t s)
-{
-    int const per_sm = p.per_sm > 0 ? p.per_sm : 1;
-    int const ix = p.g.n0 - 2;
-    int const iy = p.g.n1 - 2;
-    int const iz = p.g.n2 - 2;
-    if (ix <= 0 || iy <= 0 || iz <= 0) {
-        return cudaSuccess; // no interior cell
-    }
-    p.tiles_x = (ix + f32col::TX - 1) / f32col::TX;
-    p.tiles_y = (iy + f32col::TY - 1) / f32col::TY;
-    long long const slots = static_cast<long long>(sms) * per_sm;
-    if (p.kchunk <= 0) {
-        p.kchunk = choose_kchunk(p.tiles_x * p.tiles_y, iz, slots);
-    }
-    int const kchunks = (iz + p.kchunk - 1) / p.kchunk;
-    long long const nwork = static_cast<long long>(p.tiles_x) * p.tiles_y * kchunks;
-    p.nwork = static_cast<int>(nwork);
-    long long const grid = slots < nwork ? slots : nwork;
-    // equal face areas (cubic cells) give equal update coefficients dt/dv * ds_d
-    if (p.ds0 == p.ds1 && p.ds1 == p.ds2) {
-        f32col::f32_step_kernel<COMP, true><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
-    } else {
-        f32col::f32_step_kernel<COMP, false><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
-    }
-    return cudaGetLastError();
-}
 
 template <class T, int MODE, bool TMA, int COMP>
 struct FluxKernel {
@@ -1424,30 +842,12 @@ struct BatchKernel {
     }
 };
 
-// The column engine as the 32 x 8 shape of the FP32 batch (states without low words).
-template <int COMP>
-struct ColBatchKernel {
-    static cudaError_t configure(int* per_sm)
-    {
-        int n = 0;
-        cudaError_t const e =
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_batch_kernel<COMP>, f32col::NT, 0);
-        *per_sm = n < 1 ? 1 : n;
-        return e;
-    }
-    static cudaError_t launch(BatchParams<float> const& b, int grid, cudaStream_t s)
-    {
-        f32col::f32_batch_kernel<COMP><<<grid, f32col::NT, 0, s>>>(b);
-        return cudaGetLastError();
-    }
-};
-
 template <class T, int MODE, int COMP>
 cudaError_t batch_dispatch(int shape, BatchParams<T> const* b, int grid, int* per_sm, cudaStream_t s)
 {
     if constexpr (sizeof(T) == 4 && COMP != kCompHiLo) {
-        if (shape == 0) {
-            return b ? ColBatchKernel<COMP>::launch(*b, grid, s) : ColBatchKernel<COMP>::configure(per_sm);
+        if (shape == 0) { // the column engine
+            return launch_batch_f32col(COMP, b, grid, per_sm, s);
         }
     }
     switch (shape) {
@@ -1538,9 +938,9 @@ struct FluxDispatch<float> {
             // the stored low words do not fit the column engine's registers: the
             // double-float state keeps the shared-memory tile engine
             switch (comp) {
-            case kCompSum: return configure_f32col<kCompSum>(per_sm);
+            case kCompSum: return configure_step_f32col(kCompSum, per_sm);
             case kCompHiLo: return configure_flux_impl<float, kModeStepCons, false, kCompHiLo>(per_sm);
-            default: return configure_f32col<kCompNone>(per_sm);
+            default: return configure_step_f32col(kCompNone, per_sm);
             }
         }
         return configure_flux_impl<float, kModeGodunov, false, kCompNone>(per_sm);
@@ -1550,9 +950,9 @@ struct FluxDispatch<float> {
     {
         if (mode == kModeStep) {
             switch (comp) {
-            case kCompSum: return launch_f32col<kCompSum>(p, sms, s);
+            case kCompSum: return launch_step_f32col(p, kCompSum, sms, s);
             case kCompHiLo: return launch_flux_impl<float, kModeStepCons, false, kCompHiLo>(p, TmaMaps{}, sms, s);
-            default: return launch_f32col<kCompNone>(p, sms, s);
+            default: return launch_step_f32col(p, kCompNone, sms, s);
             }
         }
         return launch_flux_impl<float, kModeGodunov, false, kCompNone>(p, TmaMaps{}, sms, s);

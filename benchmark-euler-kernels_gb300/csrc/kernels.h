@@ -133,6 +133,12 @@ cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s);
 template <class T>
 cudaError_t launch_finalize_dt(SimScalars* sc, T cfl, int add_time, cudaStream_t s, const double* dt_seq = nullptr);
 
+// The FP32 step on the column engine (flux_f32.cu), comp kCompNone or kCompSum.
+cudaError_t configure_step_f32col(int comp, int* per_sm);
+cudaError_t launch_step_f32col(FluxParams<float> const& p, int comp, int sms, cudaStream_t s);
+// b == nullptr: configure and report resident CTAs per SM; otherwise launch.
+cudaError_t launch_batch_f32col(int comp, BatchParams<float> const* b, int grid, int* per_sm, cudaStream_t s);
+
 cudaError_t launch_fma_probe(int kind, int blocks, int iters, float* sink, cudaStream_t s);
 template <class T>
 cudaError_t launch_totals(CBundle<T> cons, CBundle<T> lo, Geom g, double* work, cudaStream_t s);
