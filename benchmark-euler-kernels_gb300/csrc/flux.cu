@@ -166,8 +166,11 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
                 pr = cons_pressure<COMP>(d, e, m0, m1, m2, r, p.gm1, nullptr);
                 cs = fast_sound_speed(p.gamma * pr * r);
             } else {
-                T const r = T(1) / d;
-                cs = sqrt(p.gamma * pr * r);
+                if constexpr (sizeof(T) == 8) {
+                    cs = fast_sound_speed(p.gamma * pr * rcp_faithful(d));
+                } else {
+                    cs = sqrt(p.gamma * pr * (T(1) / d));
+                }
                 e = pr * p.inv_gm1 + T(0.5) * d * (u0 * u0 + u1 * u1 + u2 * u2);
             }
         }
@@ -398,7 +401,7 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
             }
             if (MODE == kModeStep || MODE == kModeStepCons) {
                 // cons_to_prim of the new state (cons_to_prim.hpp:26-31)
-                T const r = rcp_rn(u[0]);
+                T const r = rcp_faithful(u[0]); // FP32: correctly rounded
                 T const v0 = u[2] * r;
                 T const v1 = u[3] * r;
                 T const v2 = u[4] * r;
