@@ -247,8 +247,13 @@ __device__ __forceinline__ bool finite_positive(double x)
 //    of num and den before any division.
 //  * pstar: the reference averages p_L + rc_L (ustar-u_L) and
 //    p_R + rc_R (ustar-u_R), which are equal by the definition of ustar; the
-//    upwind one is used.  The star energy term (pstar ustar - p un) then
-//    factors as (ustar - un)(p + rc ustar), which has no cancellation.
+//    upwind one is used.
+//  * the energy flux needs only e_star + pstar.  With a = S - un (already
+//    formed for rc = d a), w = ustar - un and ratio = a/(S - ustar):
+//    e_star + pstar = [a e + pstar ustar - p un + pstar (S - ustar)]/(S - ustar)
+//                   = [a (e + p) + S (pstar - p)]/(S - ustar)
+//                   = ratio (e + p) + w S d_star,
+//    since pstar - p = rc w = d a w and d_star = ratio d.
 //  * in the supersonic case the reference's ratio (S-un)/(S-un) is exactly 1
 //    and its energy correction exactly 0: a select returns the upwind state.
 //  * min/max and the sign tests run on the integer pipe (order_key etc.).
@@ -262,19 +267,22 @@ __device__ __forceinline__ Flux<double> hllc_flux(Side<double> const& L, Side<do
     double const S_L = umin - cmax;
     double const S_R = umax + cmax;
 
-    double const rc_L = L.d * (S_L - L.un);
-    double const rc_R = R.d * (S_R - R.un);
+    double const a_L = S_L - L.un; // S - un of each side, <= -cmax and >= cmax
+    double const a_R = S_R - R.un;
+    double const rc_L = L.d * a_L;
+    double const rc_R = R.d * a_R;
     double const num = (R.p - L.p) + rc_L * L.un - rc_R * R.un;
     double const den = rc_L - rc_R;
 
     bool const left = product_positive(num, den); // ustar > 0
     double const S = left ? S_L : S_R;
+    double const qa = left ? a_L : a_R;
     double const qd = left ? L.d : R.d;
     double const qp = left ? L.p : R.p;
     double const qun = left ? L.un : R.un;
     double const qut1 = left ? L.ut1 : R.ut1;
     double const qut2 = left ? L.ut2 : R.ut2;
-    double const qe = left ? L.e : R.e;
+    double const qh = (left ? L.e : R.e) + qp; // e + p of the upwind side
     double const qrc = left ? rc_L : rc_R;
 
     double const M = S * den - num; // den (S - ustar)
@@ -285,18 +293,18 @@ __device__ __forceinline__ Flux<double> hllc_flux(Side<double> const& L, Side<do
     double const pstar = qp + qrc * w;
 
     bool const supersonic = product_positive(S_L, S_R);
-    double const ratio = (S - qun) * inv;
+    double const ratio = qa * inv;
     double const d_star = ratio * qd;
-    double const e_star = ratio * qe + w * (qp + qrc * ustar) * inv;
+    double const h_star = ratio * qh + w * (S * d_star); // e_star + pstar
 
     double const un_o = supersonic ? qun : ustar;
     double const ptot_o = supersonic ? qp : pstar;
     double const d_o = supersonic ? qd : d_star;
-    double const e_o = supersonic ? qe : e_star;
+    double const h_o = supersonic ? qh : h_star;
 
     Flux<double> f;
     f.d = d_o * un_o;
-    f.e = (e_o + ptot_o) * un_o;
+    f.e = h_o * un_o;
     f.n = f.d * un_o + ptot_o;
     f.t1 = f.d * qut1;
     f.t2 = f.d * qut2;
