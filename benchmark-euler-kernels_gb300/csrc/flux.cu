@@ -10,8 +10,9 @@
 //   1. face phase -- every x face and y face of plane k and every z face
 //      between planes k and k+1 is solved ONCE (the reference solves each
 //      interior face twice, once from each side, godunov.hpp:48-82); the
-//      808 faces of a 32x8 tile are spread linearly over the 256 threads
-//      (97% lane occupancy) and fluxes go to shared memory in global axes;
+//      808 faces of a 32x8 tile are spread over the 256 threads with each
+//      face family starting on a warp boundary (26 warp-passes, 97% of the
+//      lanes busy) and fluxes go to shared memory in global axes;
 //   2. cell phase -- each thread owns one column cell and applies
 //      cons -= dt/dv * sum_d ds_d (F_R - F_L) (godunov.hpp:84-90) with the
 //      face-area and dt/dv factors folded into three coefficients.  The z
@@ -49,7 +50,12 @@ struct TileLayout {
     static constexpr int NFX = (TX + 1) * TY;
     static constexpr int NFY = TX * (TY + 1);
     static constexpr int NFZ = TX * TY;
-    static constexpr int NFACE = NFX + NFY + NFZ;
+    // The face loop's index space: each face family starts on a warp
+    // boundary, so no warp splits its lanes between two families (a split
+    // warp runs the HLLC once per family, each time with part of its lanes).
+    static constexpr int NFX_W = (NFX + 31) / 32 * 32;
+    static constexpr int NFY_W = (NFY + 31) / 32 * 32;
+    static constexpr int NFACE_W = NFX_W + NFY_W + NFZ;
     static constexpr int NT = TX * TY;
     // shared memory, in T elements after a 128-byte mbarrier block
     static constexpr int Q_ELEMS = NSLOT * kFields * PLANE_PAD;
@@ -324,22 +330,28 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
         // ---- face phase
         T const* qc = slot_field<T, TX, TY, NSLOT>(smem, cur, 0);
         T const* qn = slot_field<T, TX, TY, NSLOT>(smem, nxt, 0);
-        for (int f = tid; f < L::NFACE; f += L::NT) {
-            if (f < L::NFX) {
-                int const fj = f / (TX + 1);
-                int const fi = f % (TX + 1);
-                int const a = (fj + 1) * L::HX + fi;
-                store_flux(fx, L::NFX, f, 0,
-                           hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 0), load_side<T, L::PLANE_PAD>(qc, a + 1, 0)));
-            } else if (f < L::NFX + L::NFY) {
-                int const g = f - L::NFX;
-                int const fj = g / TX;
-                int const fi = g % TX;
-                int const a = fj * L::HX + fi + 1;
-                store_flux(fy, L::NFY, g, 1,
-                           hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 1), load_side<T, L::PLANE_PAD>(qc, a + L::HX, 1)));
+        for (int f = tid; f < L::NFACE_W; f += L::NT) {
+            if (f < L::NFX_W) {
+                if (f < L::NFX) {
+                    int const fj = f / (TX + 1);
+                    int const fi = f % (TX + 1);
+                    int const a = (fj + 1) * L::HX + fi;
+                    store_flux(fx, L::NFX, f, 0,
+                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 0),
+                                         load_side<T, L::PLANE_PAD>(qc, a + 1, 0)));
+                }
+            } else if (f < L::NFX_W + L::NFY_W) {
+                int const g = f - L::NFX_W;
+                if (g < L::NFY) {
+                    int const fj = g / TX;
+                    int const fi = g % TX;
+                    int const a = fj * L::HX + fi + 1;
+                    store_flux(fy, L::NFY, g, 1,
+                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 1),
+                                         load_side<T, L::PLANE_PAD>(qc, a + L::HX, 1)));
+                }
             } else {
-                int const g = f - L::NFX - L::NFY;
+                int const g = f - L::NFX_W - L::NFY_W; // < NFZ
                 int const fj = g / TX;
                 int const fi = g % TX;
                 int const a = (fj + 1) * L::HX + fi + 1;
