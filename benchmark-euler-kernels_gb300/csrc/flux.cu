@@ -251,6 +251,7 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
     int const ti = tid % TX;
     int const tj = tid / TX;
     int const center = (tj + 1) * L::HX + ti + 1;
+    bool const cubic = p.invdx0 == p.invdx1 && p.invdx1 == p.invdx2;
     T* const smem = c.smem;
     T* const fx = c.fx;
     T* const fy = c.fy;
@@ -419,8 +420,8 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
                 T const v2 = u[4] * r;
                 T pr;
                 if (MODE == kModeStep) {
-                    T const mm = u[2] * u[2] + u[3] * u[3] + u[4] * u[4];
-                    pr = p.gm1 * u[1] - (p.half_gm1 * r) * mm; // (gamma-1)(e - |m|^2/(2 rho))
+                    T const mv = u[2] * v0 + u[3] * v1 + u[4] * v2; // |m|^2 / rho
+                    pr = p.gm1 * u[1] - p.half_gm1 * mv;              // (gamma-1)(e - |m|^2/(2 rho))
                 } else {
                     pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1, COMP == kCompHiLo ? ulo : nullptr);
                 }
@@ -434,7 +435,10 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
                     p.cs_out[o] = cs;
                 }
                 // next step's CFL wavespeed (time_step.hpp:28-33)
-                T const invdt = (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 + (cs + abs_(v2)) * p.invdx2;
+                // (cubic cells: one product instead of three)
+                T const invdt = cubic ? (T(3) * cs + abs_(v0) + abs_(v1) + abs_(v2)) * p.invdx0
+                                      : (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 +
+                                                (cs + abs_(v2)) * p.invdx2;
                 if constexpr (sizeof(T) == 4) {
                     c.wmaxf = fmaxf(c.wmaxf, invdt); // NaN never wins (fmaxf returns the other operand)
                 } else {
