@@ -733,17 +733,20 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         # Each step starts from the host and ends on the host: prim copied in
-        # from pinned memory (with prim_to_cons and the first dt on the
-        # device), one step, prim copied back to pinned memory.  Two
-        # simulations on two streams alternate, so one step's copies overlap
-        # the other's compute (a stream of independent problems).
+        # from pinned memory (with prim_to_cons, the sound speed and the first
+        # dt on the device), one step, prim copied back to pinned memory.
+        # Three simulations on three streams take the steps in turn (a stream
+        # of independent problems), so each one's copies overlap the others'
+        # compute; a simulation is reused once its previous result is in host
+        # memory.
+        nsim = 3
         host = torch.empty((5, n0, n0, n0), dtype=torch.float64, pin_memory=True)
-        outs = [torch.empty((5, n0, n0, n0), dtype=torch.float64, pin_memory=True) for _ in range(2)]
+        outs = [torch.empty((5, n0, n0, n0), dtype=torch.float64, pin_memory=True) for _ in range(nsim)]
         src = random_prim_device(torch, n0, n0, n0, seed=2)
         host.copy_(src)
         del src
         torch.cuda.synchronize()
-        streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+        streams = [torch.cuda.Stream() for _ in range(nsim)]
         sims = [E.Simulation(n0, n0, n0, GAMMA, dx, CFL, stream=st) for st in streams]
         for q, sm in enumerate(sims):  # warm-up: graph, staging paths
             sm.set_prim(host)
@@ -754,13 +757,15 @@ def run_ours(args):
         for _ in range(3):  # host-link bandwidth varies with the machine's other tenants: median of 3
             t0 = time.perf_counter()
             for step in range(args.e2e_steps):
-                sm = sims[step % 2]
+                q = step % nsim
+                sm = sims[q]
+                if step >= nsim:
+                    sm.synchronize()  # its previous result is in host memory
                 sm.set_prim(host)
                 sm.advance(1)
-                sm.get_state(prim=outs[step % 2], wait=False)
-                if step >= 1:
-                    sims[(step - 1) % 2].synchronize()  # the result of step-1 is in host memory
-            sims[(args.e2e_steps - 1) % 2].synchronize()
+                sm.get_state(prim=outs[q], wait=False)
+            for sm in sims:
+                sm.synchronize()
             runs.append(world * interior * args.e2e_steps / (time.perf_counter() - t0) / 1e9)
         for sm in sims:
             sm.close()
@@ -769,8 +774,9 @@ def run_ours(args):
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
                "how": "per step: eulr_sim_set_prim_f64 from pinned host prim (H2D, then prim_to_cons, sound speed "
                       "and first dt in one kernel), eulr_sim_advance(1), eulr_sim_get_state_async_f64 of prim to "
-                      "pinned host (D2H); two simulations on two streams alternate so copies overlap compute; "
-                      "wall clock from the first copy to the last result in host memory; median of 3 runs"}
+                      "pinned host (D2H); three simulations on three streams take the steps in turn so copies "
+                      "overlap compute; wall clock from the first copy to the last result in host memory; "
+                      "median of 3 runs"}
         del host, outs
         torch.cuda.empty_cache()
 

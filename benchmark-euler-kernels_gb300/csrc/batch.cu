@@ -313,12 +313,11 @@ int prepare_grid(eulr_batch* b, int g)
     long long const n = G.g.ncell();
     B_CUDA(cudaMemsetAsync(&b->sc[g], 0, sizeof(SimScalars), b->stream), "cudaMemsetAsync");
     if (is_f64(b)) {
-        CBundle<double> pv = cbundle_of<double>(G.prim[0]);
-        B_CUDA(launch_sound_speed<double>(pv, static_cast<double*>(G.cs[0]), n, G.gamma, b->sms, b->stream),
-               "sound speed");
-        B_CUDA(launch_invdt_max<double>(pv, n, G.gamma, 1.0 / G.dx[0], 1.0 / G.dx[1], 1.0 / G.dx[2], &b->sc[g].wmax,
+        // sound speed and first wavespeed as a loaded simulation computes them
+        B_CUDA(launch_load_prim<double>(cbundle_of<double>(G.prim[0]), Bundle<double>{}, static_cast<double*>(G.cs[0]),
+                                        n, G.gamma, 1.0 / G.dx[0], 1.0 / G.dx[1], 1.0 / G.dx[2], &b->sc[g].wmax,
                                         b->sms, b->stream),
-               "invdt");
+               "load");
         B_CUDA(launch_finalize_dt<double>(&b->sc[g], b->cfl, 0, b->stream), "finalize");
     } else {
         float const gm = static_cast<float>(G.gamma);

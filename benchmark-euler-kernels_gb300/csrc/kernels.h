@@ -95,12 +95,8 @@ cudaError_t launch_cons_to_prim(CBundle<T> cons, Bundle<T> prim, long long n, T 
 template <class T>
 cudaError_t launch_time_step(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2, T* partials,
                              int max_partials, unsigned int* counter, T* dt_out, int sms, cudaStream_t s);
-template <class T>
-cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2, unsigned long long* wmax,
-                             int sms, cudaStream_t s);
-template <class T>
-cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s);
-// prim_to_cons (when cons.f[0] is set) + sound speed + max wavespeed in one pass.
+// prim_to_cons (when cons.f[0] is set), the stored sound speed and the exact
+// first max wavespeed in one pass.
 template <class T>
 cudaError_t launch_load_prim(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma, T ix0, T ix1, T ix2,
                              unsigned long long* wmax, int sms, cudaStream_t s);

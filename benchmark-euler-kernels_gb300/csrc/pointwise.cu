@@ -10,6 +10,7 @@
 // its quotients from one reciprocal of rho.
 #include "euler_device.cuh"
 #include "kernels.h"
+#include "step_common.cuh"
 
 #include <cfloat>
 
@@ -145,34 +146,6 @@ __global__ void __launch_bounds__(256) time_step_kernel(CBundle<T> prim, long lo
     }
 }
 
-// Per-cell invdt max into an ordered-bits accumulator (used by the
-// simulation's initial reduction).
-template <class T>
-__global__ void __launch_bounds__(256) invdt_max_kernel(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2,
-                                                        unsigned long long* wmax)
-{
-    T local = T(0);
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
-         c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        T const v = cell_invdt_exact(prim.f[0][c], prim.f[1][c], prim.f[2][c], prim.f[3][c], prim.f[4][c], gamma,
-                                     ix0, ix1, ix2);
-        local = (v > local) ? v : local;
-    }
-    __shared__ T warp_best[8];
-    local = warp_max(local);
-    if ((threadIdx.x & 31) == 0) {
-        warp_best[threadIdx.x >> 5] = local;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        T b = warp_best[0];
-        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
-            b = (warp_best[w] > b) ? warp_best[w] : b;
-        }
-        atomicMax(wmax, order_bits(b));
-    }
-}
-
 // Max invdt over all cells of a cons-only FP32 state, with the pressure the
 // fused FP32 step uses (compensated states rescue low-pressure cells in FP64).
 __global__ void __launch_bounds__(256) invdt_max_cons_kernel(CBundle<float> cons, long long n, float gamma, float ix0,
@@ -208,41 +181,78 @@ __global__ void __launch_bounds__(256) invdt_max_cons_kernel(CBundle<float> cons
     }
 }
 
-// Loading a primitive state into an FP64 simulation, in one pass: cons =
-// prim_to_cons(prim) (when cons is set; as prim_to_cons_kernel), the stored
-// sound speed (as sound_speed_kernel) and the max wavespeed of the first
-// step (as invdt_max_kernel) -- bit-identical to the three kernels run one
-// after the other.
+// Loading a primitive state into an FP64 simulation or batch grid, in one
+// pass:
+//  * cons = prim_to_cons(prim) when cons is set, bit-identical to
+//    prim_to_cons_kernel;
+//  * the stored sound speed in the form the fused step stores it
+//    (fast_sound_speed of (gamma/rho) p, faithful), so a loaded state and a
+//    stepped one carry the same kind of value;
+//  * the EXACT max wavespeed of time_step.hpp:28-33 (correctly rounded divide
+//    and sqrt, cell_invdt_exact) for the first dt.  The exact wavespeed is
+//    only evaluated where it can be the max: for cells whose fast wavespeed
+//    (from the faithful sound speed, within a few ulps of the exact one) has
+//    a high word at most one below the warp's running max, i.e. lies within
+//    2^-20 of it, and for cells whose fast value is not finite.  The cell
+//    holding the exact max always qualifies, so the result is the exact max
+//    over all cells; the candidates are the running-max records of each warp,
+//    a few per thousand cells on the workloads here.
 template <class T>
 __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma,
                                                         T gm1, T rgm1, T ix0, T ix1, T ix2, unsigned long long* wmax)
 {
     T local = T(0);
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
-         c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        T const d = prim.f[0][c];
-        T const p = prim.f[1][c];
-        T const u0 = prim.f[2][c];
-        T const u1 = prim.f[3][c];
-        T const u2 = prim.f[4][c];
-        if (cons.f[0] != nullptr) {
-            T const int_e = div_by_rcp(p, gm1, rgm1);
-            T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
-            cons.f[0][c] = d;
-            cons.f[1][c] = add_rn(ke, int_e);
-            cons.f[2][c] = mul_rn(d, u0);
-            cons.f[3][c] = mul_rn(d, u1);
-            cons.f[4][c] = mul_rn(d, u2);
+    unsigned run = 0u; // the warp's running max of the fast wavespeeds' high words
+    int const lane = threadIdx.x & 31;
+    bool const cubic = ix0 == ix1 && ix1 == ix2;
+    long long const stride = static_cast<long long>(gridDim.x) * blockDim.x;
+    // warp-uniform trip count: every lane of a warp runs every iteration
+    for (long long base = blockIdx.x * static_cast<long long>(blockDim.x) + (threadIdx.x & ~31); base < n;
+         base += stride) {
+        long long const c = base + lane;
+        bool const valid = c < n;
+        T d = T(1), p = T(1), u0 = T(0), u1 = T(0), u2 = T(0);
+        if (valid) {
+            d = prim.f[0][c];
+            p = prim.f[1][c];
+            u0 = prim.f[2][c];
+            u1 = prim.f[3][c];
+            u2 = prim.f[4][c];
+            if (cons.f[0] != nullptr) {
+                T const int_e = div_by_rcp(p, gm1, rgm1);
+                T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
+                cons.f[0][c] = d;
+                cons.f[1][c] = add_rn(ke, int_e);
+                cons.f[2][c] = mul_rn(d, u0);
+                cons.f[3][c] = mul_rn(d, u1);
+                cons.f[4][c] = mul_rn(d, u2);
+            }
         }
-        T const sc = sqrt_rn(div_rn(mul_rn(gamma, p), d));
-        cs[c] = sc;
-        T const v = add_rn(add_rn(mul_rn(add_rn(sc, abs_(u0)), ix0), mul_rn(add_rn(sc, abs_(u1)), ix1)),
-                           mul_rn(add_rn(sc, abs_(u2)), ix2));
-        local = (v > local) ? v : local;
+        bool cand = valid;
+        if constexpr (sizeof(T) == 8) {
+            T const sc = fast_sound_speed((gamma * rcp_faithful(d)) * p);
+            if (valid) {
+                cs[c] = sc;
+            }
+            T const vf = cubic ? (T(3) * sc + abs_(u0) + abs_(u1) + abs_(u2)) * ix0
+                               : (sc + abs_(u0)) * ix0 + (sc + abs_(u1)) * ix1 + (sc + abs_(u2)) * ix2;
+            long long const key = dbits(vf);
+            bool const fin = valid && key >= 0 && key < 0x7ff0000000000000LL; // +0 <= vf < inf
+            unsigned const hi = fin ? static_cast<unsigned>(key >> 32) : 0u;
+            unsigned const m = __reduce_max_sync(0xffffffffu, hi);
+            run = m > run ? m : run;
+            cand = valid && (!fin || hi + 1u >= run);
+        } else if (valid) {
+            cs[c] = sqrt_rn(div_rn(mul_rn(gamma, p), d));
+        }
+        if (cand) {
+            T const v = cell_invdt_exact(d, p, u0, u1, u2, gamma, ix0, ix1, ix2);
+            local = (v > local) ? v : local; // NaN never wins
+        }
     }
     __shared__ T warp_best[8];
     local = warp_max(local);
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
         warp_best[threadIdx.x >> 5] = local;
     }
     __syncthreads();
@@ -252,16 +262,6 @@ __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<
             b = (warp_best[w] > b) ? warp_best[w] : b;
         }
         atomicMax(wmax, order_bits(b));
-    }
-}
-
-// Sound speed sqrt((gamma p)/d) of every cell (perfect_gas.hpp:15-18).
-template <class T>
-__global__ void __launch_bounds__(256) sound_speed_kernel(CBundle<T> prim, T* cs, long long n, T gamma)
-{
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
-         c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        cs[c] = sqrt_rn(div_rn(mul_rn(gamma, prim.f[1][c]), prim.f[0][c]));
     }
 }
 
@@ -336,27 +336,12 @@ cudaError_t launch_time_step(CBundle<T> prim, long long n, T gamma, T ix0, T ix1
 }
 
 template <class T>
-cudaError_t launch_invdt_max(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2, unsigned long long* wmax,
-                             int sms, cudaStream_t s)
-{
-    invdt_max_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, n, gamma, ix0, ix1, ix2, wmax);
-    return cudaGetLastError();
-}
-
-template <class T>
 cudaError_t launch_load_prim(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma, T ix0, T ix1, T ix2,
                              unsigned long long* wmax, int sms, cudaStream_t s)
 {
     T const gm1 = gamma - T(1);
     load_prim_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cons, cs, n, gamma, gm1, T(1) / gm1, ix0, ix1, ix2,
                                                           wmax);
-    return cudaGetLastError();
-}
-
-template <class T>
-cudaError_t launch_sound_speed(CBundle<T> prim, T* cs, long long n, T gamma, int sms, cudaStream_t s)
-{
-    sound_speed_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cs, n, gamma);
     return cudaGetLastError();
 }
 
@@ -381,9 +366,6 @@ cudaError_t launch_invdt_max_cons(CBundle<float> cons, long long n, float gamma,
     template cudaError_t launch_cons_to_prim<T>(CBundle<T>, Bundle<T>, long long, T, int, cudaStream_t);     \
     template cudaError_t launch_time_step<T>(CBundle<T>, long long, T, T, T, T, T*, int, unsigned int*, T*,  \
                                              int, cudaStream_t);                                             \
-    template cudaError_t launch_invdt_max<T>(CBundle<T>, long long, T, T, T, T, unsigned long long*, int,    \
-                                             cudaStream_t);                                                  \
-    template cudaError_t launch_sound_speed<T>(CBundle<T>, T*, long long, T, int, cudaStream_t);                   \
     template cudaError_t launch_load_prim<T>(CBundle<T>, Bundle<T>, T*, long long, T, T, T, T, unsigned long long*,    \
                                              int, cudaStream_t);
 
