@@ -16,7 +16,8 @@
 //   adj_prep   per cell: sound speed c and its derivatives dc/dp, dc/drho,
 //              total energy, kinetic energy per mass, and the face weight
 //              w = (dt/dv) cbar on interior cells (0 on ghosts, which the
-//              step never updates).
+//              step never updates); on cubic cells w also carries the face
+//              area ds, which the face kernel then need not apply.
 //   adj_face   per cell, its three upper faces: the HLLC solve recomputed
 //              from prim_n (nothing of the forward solve is stored), then
 //              its transpose applied to g = ds (w_R - w_L).  The cell keeps
@@ -54,8 +55,8 @@ struct AdjParams {
     AdjWork w;
     double gamma, gm1, inv_gm1;
     double ds[3];
-    double hds[3]; // ds / 2
-    double wscale; // dt / dv
+    bool unit;     // cubic cells: ds is folded into the weights
+    double wscale; // dt / dv (times ds when unit)
     int mode;
 };
 
@@ -74,7 +75,8 @@ __device__ __forceinline__ void decode(Geom const& g, long long c, int& i, int& 
 
 // Per-cell data of the reverse step for state `prim` at cell c (coordinates
 // i, j, k): sound speed and its derivatives, energies, 1/rho, and the face
-// weight (dt/dv) cbar on interior cells.
+// weight wscale cbar on interior cells (wscale = dt/dv, times ds on cubic
+// cells).
 __device__ __forceinline__ void prep_cell(AdjParams const& p, CBundle<double> const& prim, double wscale,
                                           double const cb[5], long long c, int i, int j, int k)
 {
@@ -83,11 +85,11 @@ __device__ __forceinline__ void prep_cell(AdjParams const& p, CBundle<double> co
     double const u0 = prim.f[2][c];
     double const u1 = prim.f[3][c];
     double const u2 = prim.f[4][c];
-    double const R = __drcp_rn(d * pr);
+    double const R = rcp_faithful(d * pr);
     double const inv_d = pr * R;
     double const inv_p = d * R;
     double const c2 = (p.gamma * pr) * inv_d;
-    double const cs = c2 * rsqrt(c2);
+    double const cs = sqrt_faithful(c2);
     double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
     p.w.derived[0][c] = cs;
     p.w.derived[1][c] = 0.5 * cs * inv_p;
@@ -137,6 +139,7 @@ __device__ __forceinline__ FaceSide load_side(AdjParams const& p, long long c, i
 // The face halves a cell stores: its own sum over the left halves of its three
 // upper faces (index f), and the right half of each upper face (5 + a*5 + f),
 // which belongs to the neighbour c + e_a.
+template <bool UNIT>
 __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
 {
     long long const n = p.g.ncell();
@@ -163,15 +166,15 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
                     dw[f] = p.w.weight[f][cr] - p.w.weight[f][c];
-                    any = any || dw[f] != 0.0;
+                    any = any || !adj_zero(dw[f]); // on the integer pipe
                 }
                 // a face outside the cotangent's support contributes nothing (early reverse
                 // steps: the support is the functional's region grown by one cell per step)
                 if (any) {
                     FaceSide const L = load_side(p, c, a);
                     FaceSide const R = load_side(p, cr, a);
-                    hllc_bar(L, R, dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], p.ds[a], p.hds[a], p.inv_gm1,
-                             bL, bR);
+                    hllc_bar<UNIT>(L, R, dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], p.ds[a], p.inv_gm1, bL,
+                                   bR);
                 }
             }
             self[0] += bL.r;
@@ -352,10 +355,8 @@ AdjParams make_params(CBundle<double> prim, CBundle<double> cbar, Bundle<double>
     p.ds[0] = dx1 * dx2; // uniform_mesh.hpp:33-46
     p.ds[1] = dx2 * dx0;
     p.ds[2] = dx0 * dx1;
-    for (int a = 0; a < 3; ++a) {
-        p.hds[a] = 0.5 * p.ds[a];
-    }
-    p.wscale = dt / (dx0 * dx1 * dx2);
+    p.unit = p.ds[0] == p.ds[1] && p.ds[1] == p.ds[2];
+    p.wscale = dt / (dx0 * dx1 * dx2) * (p.unit ? p.ds[0] : 1.0);
     p.mode = mode;
     return p;
 }
@@ -371,12 +372,16 @@ cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bund
     if (!prepared) {
         adj_prep_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
     }
-    adj_face_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    if (p.unit) {
+        adj_face_kernel<true><<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    } else {
+        adj_face_kernel<false><<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+    }
     CBundle<double> pv{};
     double ws_prev = 0.0;
     if (prev != nullptr && mode == kAdjStep) {
         pv = *prev;
-        ws_prev = dt_prev / (dx0 * dx1 * dx2);
+        ws_prev = dt_prev / (dx0 * dx1 * dx2) * (p.unit ? p.ds[0] : 1.0);
     }
     adj_gather_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p, pv, ws_prev);
     return cudaGetLastError();

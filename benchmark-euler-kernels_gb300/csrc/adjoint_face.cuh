@@ -17,11 +17,17 @@
 
 namespace eulr {
 
-// Correctly rounded reciprocal (the device instruction sequence on the GPU).
+// Reciprocal: correctly rounded on the host; on the GPU the faithful one of
+// the forward step (PTX rcp.approx.ftz.f64 and one third-order Newton step,
+// within one ulp), which costs three FP64 instructions.
 EULR_ADJ_FN double adj_rcp(double x)
 {
 #if defined(__CUDA_ARCH__)
-    return __drcp_rn(x);
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = __fma_rn(-x, r, 1.0);
+    e = __fma_rn(e, e, e);
+    return __fma_rn(r, e, r);
 #else
     return 1.0 / x;
 #endif
@@ -78,12 +84,13 @@ struct FaceBar {
 
 EULR_ADJ_FN void zero(FaceBar& b) { b.r = b.p = b.un = b.t1 = b.t2 = 0.0; }
 
-// Subsonic star-state branch of side Q (hllc.hpp:78-102 with S = S_Q, q = Q):
-// adds its transposed contribution for the cotangent (gd, ge, gn, gt1, gt2)
-// to gus (d/d ustar), gps (d/d pstar) and bq, and returns d/d S_Q.
-EULR_ADJ_FN double star_branch_bar(FaceSide const& q, double S, double a, double iY, double ustar,
-                                                  double pstar, double gd, double ge, double gn, double gt1,
-                                                  double gt2, double inv_gm1, double& gus, double& gps, FaceBar& bq)
+// Subsonic star-state branch of the upwind side q (hllc.hpp:78-102 with
+// S = S_q): for the cotangent (gd, ge, gn, gt1, gt2) of the face flux it SETS
+// gus (d/d ustar), gps (d/d pstar) and bq (d/d q's primitives) and returns
+// d/d S_q.  a = S_q - un_q, iY = 1/(S_q - ustar).
+EULR_ADJ_FN double star_branch_bar(FaceSide const& q, double a, double iY, double ustar, double pstar, double gd,
+                                   double ge, double gn, double gt1, double gt2, double inv_gm1, double& gus,
+                                   double& gps, FaceBar& bq)
 {
     // forward: ratio = (S - un)/(S - ustar), d_o = ratio rho, etot_o = ratio e + X/(S - ustar),
     // X = pstar ustar - p un; fluxes m = d_o ustar; (m, (etot_o + pstar) ustar, m ustar + pstar, m t1, m t2)
@@ -94,22 +101,20 @@ EULR_ADJ_FN double star_branch_bar(FaceSide const& q, double S, double a, double
     double const eo = r * q.e + Xy;
     double const m = d_o * ustar;
     double const gm = gd + gn * ustar + gt1 * q.t1 + gt2 * q.t2;
-    gus += gn * m + ge * (eo + pstar) + gm * d_o;
-    gps += gn + ge * ustar;
-    double const gE = ge * ustar;          // d/d etot_o
-    double const gdo = gm * ustar;         // d/d d_o
+    double const gE = ge * ustar;           // d/d etot_o
+    double const gdo = gm * ustar;          // d/d d_o
     double const gr = gdo * q.r + gE * q.e; // d/d ratio
-    double const geq = gE * r;             // d/d e (side total energy)
+    double const geq = gE * r;              // d/d e (side total energy)
     double const gX = gE * iY;
     double const gY = -(gE * Xy + gr * r) * iY; // d/d (S - ustar)
     double const ga = gr * iY;                  // d/d (S - un)
-    gps += gX * ustar;
-    gus += gX * pstar - gY;
-    bq.r += gdo * r + geq * q.ke;
-    bq.p += geq * inv_gm1 - gX * q.un;
-    bq.un += geq * (q.r * q.un) - gX * q.p - ga;
-    bq.t1 += gt1 * m + geq * (q.r * q.t1);
-    bq.t2 += gt2 * m + geq * (q.r * q.t2);
+    gps = gn + ge * ustar + gX * ustar;
+    gus = gn * m + ge * (eo + pstar) + gm * d_o + gX * pstar - gY;
+    bq.r = gdo * r + geq * q.ke;
+    bq.p = geq * inv_gm1 - gX * q.un;
+    bq.un = geq * (q.r * q.un) - gX * q.p - ga;
+    bq.t1 = gt1 * m + geq * (q.r * q.t1);
+    bq.t2 = gt2 * m + geq * (q.r * q.t2);
     return gY + ga;
 }
 
@@ -127,10 +132,20 @@ EULR_ADJ_FN double tie_branch_bar(FaceSide const& q, double a, double iS, double
 
 // Transposed HLLC flux of one face (hllc.hpp:50-105).  The cotangent of the
 // face flux is ds * (dd, de, dn, dt1, dt2) in the face frame (mass, energy,
-// normal and tangential momentum; hds = ds / 2); adds the cotangents of both
-// sides' primitive states to bL and bR.
+// normal and tangential momentum); with UNIT the caller has already folded
+// ds into (dd, ..., dt2) and ds is not read.  SETS the cotangents of the two
+// sides' primitive states, bL and bR.
+//
+// Written for SIMT: the upwind side q (L when ustar > 0) is selected field by
+// field instead of branching on it, so a warp whose faces point both ways
+// runs the star branch once, not twice; only the rare supersonic faces and
+// the ustar == 0 ties take their own paths.  pstar is differentiated in its
+// upwind form p_q + rc_q (ustar - un_q): the reference's mean of the two
+// sides' values is the same function wherever ustar = num/den (their
+// difference is (num - ustar den)/2), so the total derivative is the same.
+template <bool UNIT = false>
 EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, double de, double dn, double dt1,
-                          double dt2, double ds, double hds, double inv_gm1, FaceBar& bL, FaceBar& bR)
+                          double dt2, double ds, double inv_gm1, FaceBar& bL, FaceBar& bR)
 {
     // S_L = min(un_L, un_R) - max(c_L, c_R), S_R = max(un_L, un_R) + max(c_L, c_R)
     long long const kuL = adj_key(L.un), kuR = adj_key(R.un);
@@ -152,67 +167,101 @@ EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, doubl
     double const den = rcL - rcR; // rcL <= 0 <= rcR: den < 0, so ustar > 0 exactly when num < 0
     bool const left = adj_neg(num);
     bool const tie = adj_zero(num);
-    // at a tie each of the two branches takes half of the cotangent
-    double const sc = tie ? hds : ds;
-    double const gd = sc * dd, ge = sc * de, gn = sc * dn, gt1 = sc * dt1, gt2 = sc * dt2;
+    double const gd = UNIT ? dd : ds * dd;
+    double const ge = UNIT ? de : ds * de;
+    double const gn = UNIT ? dn : ds * dn;
+    double const gt1 = UNIT ? dt1 : ds * dt1;
+    double const gt2 = UNIT ? dt2 : ds * dt2;
 
+    FaceSide q; // the upwind side's fields the branches read
+    q.r = left ? L.r : R.r;
+    q.p = left ? L.p : R.p;
+    q.un = left ? L.un : R.un;
+    q.t1 = left ? L.t1 : R.t1;
+    q.t2 = left ? L.t2 : R.t2;
+    q.e = left ? L.e : R.e;
+    q.ke = left ? L.ke : R.ke;
+    double const qrc = left ? rcL : rcR;
+
+    FaceBar bq;
     if (adj_pos(SL) || adj_neg(SR)) {
-        // S_L * S_R > 0: the flux is the upwind side's physical flux (ustar > 0 picks L)
-        FaceSide const& q = left ? L : R;
-        FaceBar& bq = left ? bL : bR;
+        // S_L * S_R > 0: the flux is the upwind side's physical flux
         double const m = q.r * q.un;
         double const gm = gd + gn * q.un + gt1 * q.t1 + gt2 * q.t2;
         double const geq = ge * q.un;
-        bq.un += gn * m + ge * (q.e + q.p) + gm * q.r + geq * (q.r * q.un);
-        bq.r += gm * q.un + geq * q.ke;
-        bq.p += gn + ge * q.un + geq * inv_gm1;
-        bq.t1 += gt1 * m + geq * (q.r * q.t1);
-        bq.t2 += gt2 * m + geq * (q.r * q.t2);
+        bq.un = gn * m + ge * (q.e + q.p) + gm * q.r + geq * (q.r * q.un);
+        bq.r = gm * q.un + geq * q.ke;
+        bq.p = gn + ge * q.un + geq * inv_gm1;
+        bq.t1 = gt1 * m + geq * (q.r * q.t1);
+        bq.t2 = gt2 * m + geq * (q.r * q.t2);
+        bL.r = left ? bq.r : 0.0;
+        bL.p = left ? bq.p : 0.0;
+        bL.un = left ? bq.un : 0.0;
+        bL.t1 = left ? bq.t1 : 0.0;
+        bL.t2 = left ? bq.t2 : 0.0;
+        bR.r = left ? 0.0 : bq.r;
+        bR.p = left ? 0.0 : bq.p;
+        bR.un = left ? 0.0 : bq.un;
+        bR.t1 = left ? 0.0 : bq.t1;
+        bR.t2 = left ? 0.0 : bq.t2;
         return;
     }
 
-    double inv_den, ustar, pstar;
-    double gus = 0.0, gps = 0.0, gSL = 0.0, gSR = 0.0;
+    double inv_den, ustar, gus, gps, gS;
     if (tie) {
-        // ustar == 0: the mean of the two star branches.  With ustar = 0 the
-        // mass flux m = d_o ustar vanishes, and so does every cotangent that
-        // carries a factor ustar: each branch adds only its mass and energy
-        // terms to d/d ustar and gn to d/d pstar (star_branch_bar with ustar = 0).
-        // One reciprocal gives 1/den, 1/S_L and 1/S_R.
+        // ustar == 0: the mean of the two star branches, each taking half of
+        // the cotangent.  With ustar = 0 the mass flux m = d_o ustar
+        // vanishes, and so does every cotangent that carries a factor ustar:
+        // each branch adds only its mass and energy terms to d/d ustar and
+        // half of gn to d/d pstar (star_branch_bar with ustar = 0).  One
+        // reciprocal gives 1/den, 1/S_L and 1/S_R.
         double const P = SL * SR;
         double const Rr = adj_rcp(den * P);
         inv_den = P * Rr;
         ustar = 0.0;
-        pstar = 0.5 * (L.p + R.p - rcL * L.un - rcR * R.un);
-        gus = tie_branch_bar(L, aL, (den * SR) * Rr, pstar, gd, ge, gt1, gt2) +
-              tie_branch_bar(R, aR, (den * SL) * Rr, pstar, gd, ge, gt1, gt2);
-        gps = 2.0 * gn;
+        double const pstar = q.p - qrc * q.un; // both sides' values agree at num == 0
+        double const hd = 0.5 * gd, he = 0.5 * ge, ht1 = 0.5 * gt1, ht2 = 0.5 * gt2;
+        gus = tie_branch_bar(L, aL, (den * SR) * Rr, pstar, hd, he, ht1, ht2) +
+              tie_branch_bar(R, aR, (den * SL) * Rr, pstar, hd, he, ht1, ht2);
+        gps = gn;
+        gS = 0.0;
+        bq.r = 0.0;
+        bq.p = 0.0;
+        bq.un = 0.0;
+        bq.t1 = 0.0;
+        bq.t2 = 0.0;
     } else {
         // One reciprocal gives 1/den and 1/(S - ustar): with Z = S den - num,
         // S - ustar = Z/den, so 1/den = Z R and 1/(S - ustar) = den^2 R for R = 1/(den Z).
-        double const S0 = left ? SL : SR;
-        double const Z = S0 * den - num;
+        double const Z = (left ? SL : SR) * den - num;
         double const Rr = adj_rcp(den * Z);
         inv_den = Z * Rr;
         double const iY0 = (den * den) * Rr;
         ustar = num * inv_den;
-        pstar = 0.5 * (L.p + R.p + rcL * (ustar - L.un) + rcR * (ustar - R.un));
-        if (left) {
-            gSL = star_branch_bar(L, SL, aL, iY0, ustar, pstar, gd, ge, gn, gt1, gt2, inv_gm1, gus, gps, bL);
-        } else {
-            gSR = star_branch_bar(R, SR, aR, iY0, ustar, pstar, gd, ge, gn, gt1, gt2, inv_gm1, gus, gps, bR);
-        }
+        double const pstar = q.p + qrc * (ustar - q.un);
+        gS = star_branch_bar(q, left ? aL : aR, iY0, ustar, pstar, gd, ge, gn, gt1, gt2, inv_gm1, gus, gps, bq);
     }
 
-    // pstar = (p_L + p_R + rc_L (ustar - un_L) + rc_R (ustar - un_R)) / 2
-    double const h = 0.5 * gps;
-    bL.p += h;
-    bR.p += h;
-    double grcL = h * (ustar - L.un);
-    double grcR = h * (ustar - R.un);
-    gus += h * (rcL + rcR);
-    bL.un -= h * rcL;
-    bR.un -= h * rcR;
+    // pstar = p_q + rc_q (ustar - un_q)
+    bq.p += gps;
+    bq.un -= gps * qrc;
+    gus += gps * qrc;
+    double const grcq = gps * (ustar - q.un);
+    // to the upwind side
+    bL.r = left ? bq.r : 0.0;
+    bL.p = left ? bq.p : 0.0;
+    bL.un = left ? bq.un : 0.0;
+    bL.t1 = left ? bq.t1 : 0.0;
+    bL.t2 = left ? bq.t2 : 0.0;
+    bR.r = left ? 0.0 : bq.r;
+    bR.p = left ? 0.0 : bq.p;
+    bR.un = left ? 0.0 : bq.un;
+    bR.t1 = left ? 0.0 : bq.t1;
+    bR.t2 = left ? 0.0 : bq.t2;
+    double grcL = left ? grcq : 0.0;
+    double grcR = left ? 0.0 : grcq;
+    double gSL = left ? gS : 0.0;
+    double gSR = left ? 0.0 : gS;
     // ustar = num / den
     double const gnum = gus * inv_den;
     double const gden = -gnum * ustar;
@@ -231,18 +280,10 @@ EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, doubl
     gSR += gaR;
     bL.un -= gaL;
     bR.un -= gaR;
-    // S_L = umin - cmax, S_R = umax + cmax
-    if (u_lt) {
-        bL.un += gSL;
-        bR.un += gSR;
-    } else if (u_gt) {
-        bR.un += gSL;
-        bL.un += gSR;
-    } else {
-        double const hs = 0.5 * (gSL + gSR);
-        bL.un += hs;
-        bR.un += hs;
-    }
+    // S_L = umin - cmax, S_R = umax + cmax (equal un: half to each side)
+    double const hs = 0.5 * (gSL + gSR);
+    bL.un += u_lt ? gSL : (u_gt ? gSR : hs);
+    bR.un += u_lt ? gSR : (u_gt ? gSL : hs);
     double const gc = gSR - gSL;
     double const gcL = c_lt ? 0.0 : (c_gt ? gc : 0.5 * gc);
     double const gcR = gc - gcL;

@@ -7,14 +7,16 @@
 // Each is recomputed from its checkpoint with the recorded dt sequence --
 // bit-identical to the forward pass -- keeping prim_n of every step in the
 // segment, and then the reverse steps (adjoint.cu) run from its last step
-// down to its first.  A segment of k steps needs prim_n for its k steps, so
-// it recomputes k-1 steps (none when k = 1); the final state is kept from
-// the forward pass.  Memory: ceil(nsteps/k) checkpoints of 11 fields plus k
-// primitive states, instead of nsteps states.
+// down to its first.  A segment of k steps needs prim_n for its k steps:
+// the first is the checkpoint's own prim, and the k-1 recomputed steps
+// write theirs into the segment buffer from the step kernels themselves (a
+// second prim output), so recording costs no copies.  The final state is
+// kept from the forward pass.  Memory: ceil(nsteps/k) checkpoints of 11
+// fields plus k-1 primitive states, instead of nsteps states.
 //
 // Device memory (one allocation, fields of n0*n1*n2 doubles padded to 256 B):
 //   checkpoints   nckpt x 11
-//   segment prims k x 5
+//   segment prims (k-1) x 5
 //   cbar 5, prim0_bar 5, final prim_bar 5, final prim 5
 //   reverse-step workspace kAdjWorkFields
 #include "euler_gb300.h"
@@ -45,8 +47,12 @@ struct eulr_adjoint {
 
     double* at(size_t index) const { return reinterpret_cast<double*>(static_cast<char*>(slab) + field * index); }
     double* ckpt(int c, int f) const { return at(static_cast<size_t>(c) * 11 + f); }
-    double* seg(int n, int f) const { return at(static_cast<size_t>(nckpt) * 11 + static_cast<size_t>(n) * 5 + f); }
-    size_t tail() const { return static_cast<size_t>(nckpt) * 11 + static_cast<size_t>(every) * 5; }
+    // prim of the n-th step after a segment's checkpoint, n = 1 .. every-1
+    double* seg(int n, int f) const
+    {
+        return at(static_cast<size_t>(nckpt) * 11 + static_cast<size_t>(n - 1) * 5 + f);
+    }
+    size_t tail() const { return static_cast<size_t>(nckpt) * 11 + static_cast<size_t>(every - 1) * 5; }
     double* cbar(int f) const { return at(tail() + f); }
     double* pbar0(int f) const { return at(tail() + 5 + f); }
     double* pbarT(int f) const { return at(tail() + 10 + f); }
@@ -335,15 +341,14 @@ int eulr_adjoint_backward(eulr_adjoint* a, eulr_prim_cf64 prim_final_bar, eulr_p
             src[f] = a->ckpt(c, f);
         }
         ADJ_TRY(eulr::sim_restore(a->sim, src, s0));
-        for (int n = s0; n < s1; ++n) {
+        // prim of steps s0+1 .. s1-1, written by the recomputing step kernels
+        // themselves (prim of step s0 is the checkpoint's)
+        for (int n = s0 + 1; n < s1; ++n) {
             double* dst[5];
             for (int f = 0; f < 5; ++f) {
                 dst[f] = a->seg(n - s0, f);
             }
-            ADJ_TRY(eulr::sim_snapshot(a->sim, dst, 5));
-            if (n + 1 < s1) {
-                ADJ_TRY(eulr_sim_advance(a->sim, 1));
-            }
+            ADJ_TRY(eulr::sim_advance_recording(a->sim, dst));
         }
         ADJ_CUDA(cudaEventRecord(rec.b, a->stream), "cudaEventRecord");
         ADJ_CUDA(cudaEventRecord(rev.a, a->stream), "cudaEventRecord");
@@ -360,8 +365,8 @@ int eulr_adjoint_backward(eulr_adjoint* a, eulr_prim_cf64 prim_final_bar, eulr_p
             double* pn[5];
             double* pp[5];
             for (int f = 0; f < 5; ++f) {
-                pn[f] = a->seg(n - s0, f);
-                pp[f] = n - 1 >= s0 ? a->seg(n - 1 - s0, f) : nullptr;
+                pn[f] = n == s0 ? a->ckpt(c, f) : a->seg(n - s0, f);
+                pp[f] = n - 1 > s0 ? a->seg(n - 1 - s0, f) : (n - 1 == s0 ? a->ckpt(c, f) : nullptr);
             }
             int const mode = n == 0 ? kAdjInitial : kAdjStep;
             CBundle<double> const prev = cb(pp);

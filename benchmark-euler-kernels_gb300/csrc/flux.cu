@@ -432,6 +432,13 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
                     p.prim_out.f[2][o] = v0;
                     p.prim_out.f[3][o] = v1;
                     p.prim_out.f[4][o] = v2;
+                    if (p.prim_rec.f[0] != nullptr) { // a second copy, for a recording caller
+                        p.prim_rec.f[0][o] = u[0];
+                        p.prim_rec.f[1][o] = pr;
+                        p.prim_rec.f[2][o] = v0;
+                        p.prim_rec.f[3][o] = v1;
+                        p.prim_rec.f[4][o] = v2;
+                    }
                     p.cs_out[o] = cs;
                 }
                 // next step's CFL wavespeed (time_step.hpp:28-33)
@@ -686,6 +693,13 @@ __device__ __forceinline__ void ghost_shell_body(GhostParams<T> const& p)
             p.prim_out.f[2][o] = u0;
             p.prim_out.f[3][o] = u1;
             p.prim_out.f[4][o] = u2;
+            if (p.prim_rec.f[0] != nullptr) {
+                p.prim_rec.f[0][o] = d;
+                p.prim_rec.f[1][o] = pr;
+                p.prim_rec.f[2][o] = u0;
+                p.prim_rec.f[3][o] = u1;
+                p.prim_rec.f[4][o] = u2;
+            }
             p.cs_out[o] = sqrt_rn(div_rn(mul_rn(p.gamma, pr), d));
         }
         T v;

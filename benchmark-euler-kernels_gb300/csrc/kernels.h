@@ -44,6 +44,7 @@ struct FluxParams {
     CBundle<T> cons_in;  // read (centre; step mode also e with halo)
     Bundle<T> cons_out;  // written (interior); may equal cons_in in godunov mode
     Bundle<T> prim_out;  // step mode: cons_to_prim of the new state (interior)
+    Bundle<T> prim_rec;  // step mode, when set: a second copy of prim_out (the adjoint's recompute)
     T* cs_out;           // step mode: sound speed of the new state (interior)
     T gamma, gm1, inv_gm1, half_gm1;
     T ds0, ds1, ds2;     // face areas dx1*dx2, dx2*dx0, dx0*dx1
@@ -80,6 +81,7 @@ struct GhostParams {
     Bundle<T> lo_out;
     int comp;         // kComp* of a cons-only FP32 state (prim_out unset)
     Bundle<T> prim_out;
+    Bundle<T> prim_rec; // when set: a second copy of prim_out
     T* cs_out;
     T gamma, gm1;
     T invdx0, invdx1, invdx2;
@@ -186,5 +188,8 @@ int sim_fail(int status, const char* msg);
 int sim_restore(eulr_sim* s, const double* const* src, long long step);
 // The stream the simulation's work runs on (its own when created with NULL).
 cudaStream_t sim_stream(eulr_sim* s);
+// One step of a loaded FP64 simulation (as eulr_sim_advance(s, 1)) whose
+// kernels also write the new prim (every cell) into dst[0..4].
+int sim_advance_recording(eulr_sim* s, double* const* dst);
 
 } // namespace eulr

@@ -102,6 +102,7 @@ struct eulr_sim {
     double* dt_seq = nullptr;  // device copy of a fixed dt sequence (owned), or null
     long long dt_seq_len = 0;
     long long host_steps = 0;  // steps taken since the state was loaded (host-side count)
+    double* rec[5] = {};       // set only inside sim_advance_recording: a second prim output
 };
 
 namespace {
@@ -222,6 +223,9 @@ GhostParams<T> ghost_params(eulr_sim* s, int in, int out, unsigned long long* wm
     if (is_f64(s)) {
         gp.prim_out = bundle_of<T>(s->prim[out]);
         gp.cs_out = static_cast<T*>(s->cs[out]);
+        if (s->rec[0] != nullptr) {
+            gp.prim_rec = bundle_of<T>(reinterpret_cast<void* const*>(s->rec));
+        }
     }
     gp.comp = s->comp;
     gp.gamma = gamma;
@@ -263,6 +267,9 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
         p.cs = static_cast<const T*>(s->cs[in]);
         p.prim_out = bundle_of<T>(s->prim[out]);
         p.cs_out = static_cast<T*>(s->cs[out]);
+        if (s->rec[0] != nullptr) {
+            p.prim_rec = bundle_of<T>(reinterpret_cast<void* const*>(s->rec));
+        }
     }
     p.cons_in = cbundle_of<T>(s->cons[in]);
     p.cons_out = bundle_of<T>(s->cons[out]);
@@ -443,6 +450,32 @@ int sim_snapshot(eulr_sim* s, double* const* dst, int nfields)
 }
 
 cudaStream_t sim_stream(eulr_sim* s) { return s->stream; }
+
+int sim_advance_recording(eulr_sim* s, double* const* dst)
+{
+    SIM_TRY(check_sim(s));
+    if (!is_f64(s) || !s->loaded) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "recording needs a loaded FP64 simulation");
+    }
+    if (s->dt_seq != nullptr && s->host_steps + 1 > s->dt_seq_len) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "advance past the end of the fixed dt sequence");
+    }
+    for (int f = 0; f < 5; ++f) {
+        if (dst[f] == nullptr) {
+            return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "recording field is NULL");
+        }
+        s->rec[f] = dst[f];
+    }
+    int const in = s->cur;
+    int const st = enqueue_step(s, in); // launched directly: the captured graph has no second output
+    for (int f = 0; f < 5; ++f) {
+        s->rec[f] = nullptr;
+    }
+    SIM_TRY(st);
+    s->cur = 1 - in;
+    s->host_steps += 1;
+    return EULR_SUCCESS;
+}
 
 int sim_restore(eulr_sim* s, const double* const* src, long long step)
 {

@@ -19,7 +19,9 @@ extern "C" void host_godunov_adjoint(const double* const* prim, const double* co
     long long const s1 = n0, s2 = static_cast<long long>(n0) * n1, n = s2 * n2;
     double const inv_gm1 = 1.0 / (gamma - 1.0);
     double const ds[3] = {dx1 * dx2, dx2 * dx0, dx0 * dx1};
-    double const wscale = dt / (dx0 * dx1 * dx2);
+    // cubic cells: the face area is folded into the weights, as the GPU kernel does
+    bool const unit = ds[0] == ds[1] && ds[1] == ds[2];
+    double const wscale = dt / (dx0 * dx1 * dx2) * (unit ? ds[0] : 1.0);
     std::vector<double> der(static_cast<size_t>(n) * 5), w(static_cast<size_t>(n) * 5);
     auto interior = [&](int i, int j, int k) {
         return i >= 1 && i < n0 - 1 && j >= 1 && j < n1 - 1 && k >= 1 && k < n2 - 1;
@@ -77,8 +79,13 @@ extern "C" void host_godunov_adjoint(const double* const* prim, const double* co
             FaceBar bL, bR;
             zero(bL);
             zero(bR);
-            hllc_bar(side(c, a), side(cr, a), dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], ds[a], 0.5 * ds[a],
-                     inv_gm1, bL, bR);
+            if (unit) {
+                hllc_bar<true>(side(c, a), side(cr, a), dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], ds[a], inv_gm1,
+                               bL, bR);
+            } else {
+                hllc_bar<false>(side(c, a), side(cr, a), dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], ds[a], inv_gm1,
+                                bL, bR);
+            }
             double const lv[5] = {bL.r, bL.p, bL.un, bL.t1, bL.t2};
             double const rv[5] = {bR.r, bR.p, bR.un, bR.t1, bR.t2};
             int const map[5] = {0, 1, 2 + a, 2 + b, 2 + e};

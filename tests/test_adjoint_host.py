@@ -137,7 +137,10 @@ def test_tie_rule_is_the_central_difference_limit(tlm):
 
 
 @pytest.mark.parametrize("case", ["generic", "rest"])
-def test_face_adjoint_dot_product(tlm, host_adj, case):
+@pytest.mark.parametrize("dx", [DX, (0.1,) * 3], ids=["anisotropic", "cubic"])
+def test_face_adjoint_dot_product(tlm, host_adj, case, dx):
+    """<J^T w, v> = <w, J v>; cubic cells take the path with the face area
+    folded into the weights."""
     O = tlm
     rng = np.random.default_rng(7)
     prim = O.random_prim(9, 8, 7, seed=11) if case == "generic" else rest_state(O, 9, 8, 7, seed=11)
@@ -145,8 +148,8 @@ def test_face_adjoint_dot_product(tlm, host_adj, case):
     for _ in range(3):
         w = rng.normal(size=prim.shape)
         v = rng.normal(size=prim.shape)
-        _, jv = O.tlm_godunov(prim, v, cons, np.zeros_like(cons), GAMMA, DX, DT)
-        lhs = float(np.sum(host_adj(prim, w) * v))
+        _, jv = O.tlm_godunov(prim, v, cons, np.zeros_like(cons), GAMMA, dx, DT)
+        lhs = float(np.sum(host_adj(prim, w, dx=dx) * v))
         rhs = float(np.sum(w * jv))
         assert abs(lhs - rhs) <= 1e-13 * abs(rhs)
 
