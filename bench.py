@@ -57,10 +57,10 @@ CFL = 0.4
 FLOPS_PER_CELL_DEFAULT = None
 
 # DRAM bytes (read + write) per interior cell of the fused FP64 kernel, from
-# one ncu capture at 192^3 (profiles/flux_step_f64_192.md: 673 MB + 582 MB over
+# one ncu capture at 192^3 (profiles/flux_step_f64_192.md: 672 MB + 582 MB over
 # 7.08 M interior cells); the kernel streams each plane once, so traffic
 # scales with cells.
-FLUX_F64_DRAM_BYTES_PER_CELL = 177.3
+FLUX_F64_DRAM_BYTES_PER_CELL = 177.1
 
 
 def parse():
@@ -608,10 +608,18 @@ def time_ops(torch, E, prim, n_int, fpc=None, fp64_peak=None, hbm_peak=None):
             rec = out[name]
             rec["flops_per_cell"] = per_cell
             rec["fp64_tflops"] = per_cell * units / (rec["ms"] * 1e-3) / 1e12
-            if fp64_peak:
+            if fp64_peak and name != "time_step":
                 rec["fp64_frac"] = rec["fp64_tflops"] * 1e12 / fp64_peak
             if hbm_peak:
                 rec["hbm_frac"] = rec["gb_s"] / hbm_peak
+    # the roofline that bounds each operator on GB300 (profiles/pointwise_ops_f64_256.md)
+    for name in ("prim_to_cons", "cons_to_prim", "godunov"):
+        out[name]["bound"] = "fp64"
+    out["time_step"]["bound"] = "hbm"
+    out["time_step"]["note"] = ("the max wavespeed is screened by an FP32 estimate built on the integer and FP32 "
+                                "pipes; the exact FP64 wavespeed (correctly rounded divide and sqrt) is evaluated "
+                                "only for the cells that can hold the max, so the dt is the reference's bit for bit "
+                                "and the kernel streams its 40 B per cell: no FP64 fraction applies")
     return out
 
 
@@ -686,7 +694,7 @@ def run_ours(args):
             "kernel": "flux_tile_kernel<double, step>", "kernel_ms": flux_ms,
             "step_ms_sum_of_launches": step_ms_launches,
             "traffic": FLUX_F64_DRAM_BYTES_PER_CELL * interior,
-            "traffic_note": "dram bytes read+write per launch: 177.3 B per interior cell from an ncu capture at "
+            "traffic_note": "dram bytes read+write per launch: 177.1 B per interior cell from an ncu capture at "
                             "192^3 (profiles/flux_step_f64_192.md), scaled by cells"}
     if fpc:
         fl = fpc["fused_step_fp64"] * interior

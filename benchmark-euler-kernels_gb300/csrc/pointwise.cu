@@ -87,22 +87,111 @@ __global__ void __launch_bounds__(256) cons_to_prim_kernel(CBundle<T> cons, Bund
     }
 }
 
+// ------------------------------------------ exact max wavespeed, screened
+// The CFL step needs the max over cells of the reference's wavespeed
+// (time_step.hpp:28-33; cell_invdt_exact: a correctly rounded FP64 division
+// and square root per cell, about 25 FP64 issue slots), exactly.  But the
+// exact value is needed only where it can be the max, so an FP32 estimate
+// screens the cells, with no FP64 instruction at all: its inputs are built
+// from the doubles' high words on the integer pipe (the mantissa truncated to
+// 20 bits, a relative error in (-2^-20, 0]) and the rest runs on the FP32
+// pipe.  Where rho, p and gamma p/rho lie in [1e-30, 1e30] and the estimate
+// is at most 1e30, its relative error is below 2^-20 + 5 * 2^-24 to first
+// order: p/rho carries under 2^-20 (both truncations go toward zero), the
+// square root halves it, |u| carries under 2^-20, and gamma, 1/dx and eight
+// FP32 operations add 2^-24 each along any path.  Two estimates can thus
+// misorder cells by at most 2.7 * 2^-20 relative, 42 FP32 ulps; a cell is
+// evaluated exactly when its estimate is within 128 ulps of the warp's
+// running max of estimates.  Every other cell -- NaN, infinite or
+// out-of-range values -- is always evaluated exactly.  So the cell holding
+// the exact max is always evaluated, and the max of the exact values over
+// the evaluated cells is the exact max.  The evaluated cells are essentially
+// each warp's running-max records: a few per ten thousand on random states.
+struct WaveScreen {
+    float g, ix0, ix1, ix2;
+    bool on;        // gamma and 1/dx in FP32's safe range: screening is sound
+    unsigned run;   // the warp's running max of the estimates' bit patterns
+
+    __device__ __forceinline__ static bool in_range(float x) { return x >= 1e-30f && x <= 1e30f; }
+
+    // x with its mantissa truncated to 20 bits, from the high word alone: 0
+    // below FP32's normal range, infinity above it (and for NaN).
+    __device__ __forceinline__ static float high_word_float(double x)
+    {
+        unsigned const hi = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(x)) >> 32);
+        int const e = static_cast<int>((hi >> 20) & 0x7ffu) - (1023 - 127);
+        unsigned const mag = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : (static_cast<unsigned>(e) << 23) | ((hi & 0xfffffu) << 3));
+        return __uint_as_float((hi & 0x80000000u) | mag);
+    }
+
+    __device__ __forceinline__ WaveScreen(double gamma, double x0, double x1, double x2)
+        : g(static_cast<float>(gamma)), ix0(static_cast<float>(x0)), ix1(static_cast<float>(x1)),
+          ix2(static_cast<float>(x2)), run(0u)
+    {
+        on = in_range(g) && in_range(ix0) && in_range(ix1) && in_range(ix2);
+    }
+
+    // Warp-collective (all 32 lanes call it together): true when this lane's
+    // cell (if valid) needs its exact wavespeed.
+    __device__ __forceinline__ bool exact_needed(bool valid, double d, double p, double u0, double u1, double u2)
+    {
+        float const d32 = high_word_float(d);
+        float const p32 = high_word_float(p);
+        float const x32 = __fdiv_rn(g * p32, d32);
+        float const c32 = __fsqrt_rn(x32);
+        float const v32 = (c32 + fabsf(high_word_float(u0))) * ix0 + (c32 + fabsf(high_word_float(u1))) * ix1 +
+                          (c32 + fabsf(high_word_float(u2))) * ix2;
+        bool const sure = on && in_range(d32) && in_range(p32) && in_range(x32) && v32 <= 1e30f;
+        unsigned const key = (valid && sure) ? __float_as_uint(v32) : 0u;
+        unsigned const m = __reduce_max_sync(0xffffffffu, key);
+        run = m > run ? m : run;
+        return valid && (!sure || key + 128u >= run);
+    }
+};
+
 // --------------------------------------------------------------- time_step
 // time_step.hpp:22-39.  The reference takes min over cells of 1/invdt; since
 // correctly rounded division is monotonic, min_c RN(1/x_c) = RN(1/max_c x_c),
 // so the kernel reduces max(invdt) (exact, order-free) and divides once.
-// NaN never wins (the reference's Kokkos::min skips it) and an all-zero grid
-// returns the reduction identity T's max, as the reference's Min reducer does.
+// FP64: the max is screened (WaveScreen), so the kernel reads 40 B per cell
+// and issues FP64 instructions only for the few cells evaluated exactly; the
+// dt is still the reference's bit for bit.  NaN never wins (the reference's Kokkos::min
+// skips it) and an all-zero grid returns the reduction identity T's max, as
+// the reference's Min reducer does.
 template <class T>
 __global__ void __launch_bounds__(256) time_step_kernel(CBundle<T> prim, long long n, T gamma, T ix0, T ix1, T ix2,
                                                         T* partials, unsigned int* counter, T* dt_out)
 {
     T local = T(0);
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
-         c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        T const v = cell_invdt_exact(prim.f[0][c], prim.f[1][c], prim.f[2][c], prim.f[3][c], prim.f[4][c], gamma,
-                                     ix0, ix1, ix2);
-        local = (v > local) ? v : local;
+    if constexpr (sizeof(T) == 8) {
+        WaveScreen screen(gamma, ix0, ix1, ix2);
+        int const lane = threadIdx.x & 31;
+        long long const stride = static_cast<long long>(gridDim.x) * blockDim.x;
+        // warp-uniform trip count: every lane of a warp runs every iteration
+        for (long long base = blockIdx.x * static_cast<long long>(blockDim.x) + (threadIdx.x & ~31); base < n;
+             base += stride) {
+            long long const c = base + lane;
+            bool const valid = c < n;
+            T d = T(1), p = T(1), u0 = T(0), u1 = T(0), u2 = T(0);
+            if (valid) {
+                d = prim.f[0][c];
+                p = prim.f[1][c];
+                u0 = prim.f[2][c];
+                u1 = prim.f[3][c];
+                u2 = prim.f[4][c];
+            }
+            if (screen.exact_needed(valid, d, p, u0, u1, u2)) {
+                T const v = cell_invdt_exact(d, p, u0, u1, u2, gamma, ix0, ix1, ix2);
+                local = (v > local) ? v : local;
+            }
+        }
+    } else {
+        for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+             c += static_cast<long long>(gridDim.x) * blockDim.x) {
+            T const v = cell_invdt_exact(prim.f[0][c], prim.f[1][c], prim.f[2][c], prim.f[3][c], prim.f[4][c], gamma,
+                                         ix0, ix1, ix2);
+            local = (v > local) ? v : local;
+        }
     }
     __shared__ T warp_best[8];
     __shared__ bool is_last;
@@ -188,23 +277,16 @@ __global__ void __launch_bounds__(256) invdt_max_cons_kernel(CBundle<float> cons
 //  * the stored sound speed in the form the fused step stores it
 //    (fast_sound_speed of (gamma/rho) p, faithful), so a loaded state and a
 //    stepped one carry the same kind of value;
-//  * the EXACT max wavespeed of time_step.hpp:28-33 (correctly rounded divide
-//    and sqrt, cell_invdt_exact) for the first dt.  The exact wavespeed is
-//    only evaluated where it can be the max: for cells whose fast wavespeed
-//    (from the faithful sound speed, within a few ulps of the exact one) has
-//    a high word at most one below the warp's running max, i.e. lies within
-//    2^-20 of it, and for cells whose fast value is not finite.  The cell
-//    holding the exact max always qualifies, so the result is the exact max
-//    over all cells; the candidates are the running-max records of each warp,
-//    a few per thousand cells on the workloads here.
+//  * the EXACT max wavespeed of time_step.hpp:28-33 for the first dt, with
+//    the exact per-cell value evaluated only where WaveScreen says it can be
+//    the max.
 template <class T>
 __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma,
                                                         T gm1, T rgm1, T ix0, T ix1, T ix2, unsigned long long* wmax)
 {
     T local = T(0);
-    unsigned run = 0u; // the warp's running max of the fast wavespeeds' high words
+    WaveScreen screen(gamma, ix0, ix1, ix2);
     int const lane = threadIdx.x & 31;
-    bool const cubic = ix0 == ix1 && ix1 == ix2;
     long long const stride = static_cast<long long>(gridDim.x) * blockDim.x;
     // warp-uniform trip count: every lane of a warp runs every iteration
     for (long long base = blockIdx.x * static_cast<long long>(blockDim.x) + (threadIdx.x & ~31); base < n;
@@ -230,18 +312,10 @@ __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<
         }
         bool cand = valid;
         if constexpr (sizeof(T) == 8) {
-            T const sc = fast_sound_speed((gamma * rcp_faithful(d)) * p);
             if (valid) {
-                cs[c] = sc;
+                cs[c] = fast_sound_speed((gamma * rcp_faithful(d)) * p);
             }
-            T const vf = cubic ? (T(3) * sc + abs_(u0) + abs_(u1) + abs_(u2)) * ix0
-                               : (sc + abs_(u0)) * ix0 + (sc + abs_(u1)) * ix1 + (sc + abs_(u2)) * ix2;
-            long long const key = dbits(vf);
-            bool const fin = valid && key >= 0 && key < 0x7ff0000000000000LL; // +0 <= vf < inf
-            unsigned const hi = fin ? static_cast<unsigned>(key >> 32) : 0u;
-            unsigned const m = __reduce_max_sync(0xffffffffu, hi);
-            run = m > run ? m : run;
-            cand = valid && (!fin || hi + 1u >= run);
+            cand = screen.exact_needed(valid, d, p, u0, u1, u2);
         } else if (valid) {
             cs[c] = sqrt_rn(div_rn(mul_rn(gamma, p), d));
         }

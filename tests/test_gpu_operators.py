@@ -115,6 +115,39 @@ def test_time_step_edge_values(cuda, euler, oracle_lib):
     assert got == ref
 
 
+@pytest.mark.parametrize("case", ["near_ties", "wide_range", "large_random"])
+def test_time_step_screened_max_is_exact(cuda, euler, oracle_lib, case):
+    """time_step and a simulation's first dt evaluate the exact wavespeed
+    only where an FP32 estimate says it can be the max; dt stays the
+    reference's bit for bit on states built against that screen: wavespeeds
+    a few ulps apart everywhere, values far outside FP32's range (always
+    evaluated exactly), and a large grid."""
+    O = oracle_lib
+    rng = np.random.default_rng(31)
+    if case == "near_ties":
+        shape = (40, 37, 33)
+        prim = np.empty((5,) + shape[::-1])
+        prim[0] = 1.0 + rng.integers(-8, 9, prim.shape[1:]) * 2.0 ** -52
+        prim[1] = 1.0 + rng.integers(-8, 9, prim.shape[1:]) * 2.0 ** -52
+        prim[2:] = 0.3
+    elif case == "wide_range":
+        shape = (31, 29, 27)
+        prim = O.random_prim(*shape, seed=5)
+        prim[0] *= 10.0 ** rng.uniform(-40, 40, prim.shape[1:])
+        prim[1] *= 10.0 ** rng.uniform(-40, 40, prim.shape[1:])
+        prim[2:] *= 10.0 ** rng.uniform(-20, 20, prim.shape[1:])
+    else:
+        shape = (130, 130, 130)
+        prim = O.random_prim(*shape, seed=6)
+    g, dx = 1.4, (0.01, 0.01, 0.01)
+    ref = O.time_step(prim, g, dx)
+    assert euler.time_step(_t(cuda, prim), g, dx).item() == ref
+    host = cuda.from_numpy(prim).pin_memory()
+    with euler.Simulation(*shape, g, dx, 0.4) as sim:
+        sim.set_prim(host)
+        assert sim.time()[1] == 0.4 * ref
+
+
 def test_canary_guard_bands(cuda, euler, oracle_lib):
     """Every kernel writes only inside its arrays: fields are carved out of
     one buffer with canary gaps that must survive a full operator round."""
