@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kThreads) c2p_bar_kernel(CBundle<double> prim,
         double const d = prim.f[0][c];
         double const u0 = prim.f[2][c], u1 = prim.f[3][c], u2 = prim.f[4][c];
         double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
-        double const inv_d = __drcp_rn(d);
+        double const inv_d = rcp_faithful(d);
         double const b0 = pbar.f[0][c], b2 = pbar.f[2][c], b3 = pbar.f[3][c], b4 = pbar.f[4][c];
         double const gp = pbar.f[1][c] * gm1;
         double r[5];
