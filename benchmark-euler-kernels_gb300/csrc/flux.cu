@@ -9,10 +9,12 @@
 // (TX+2) x (TY+2) plane with its one-cell halo.  Per plane:
 //   1. face phase -- every x face and y face of plane k and every z face
 //      between planes k and k+1 is solved ONCE (the reference solves each
-//      interior face twice, once from each side, godunov.hpp:48-82); the
-//      808 faces of a 32x8 tile are spread over the 256 threads with each
-//      face family starting on a warp boundary (26 warp-passes, 97% of the
-//      lanes busy) and fluxes go to shared memory in global axes;
+//      interior face twice, once from each side, godunov.hpp:48-82).  The
+//      x, y and z faces share one index space, and each face's family,
+//      cells and axis permutation are chosen by selects, so a warp whose
+//      lanes straddle two families still runs the HLLC once: the 800 faces
+//      of a 16x16 tile take exactly 25 warp-passes.  Fluxes go to shared
+//      memory in global axes;
 //   2. cell phase -- each thread owns one column cell and applies
 //      cons -= dt/dv * sum_d ds_d (F_R - F_L) (godunov.hpp:84-90) with the
 //      face-area and dt/dv factors folded into three coefficients.  The z
@@ -22,7 +24,7 @@
 // atomicMax per CTA, so dt never leaves the device.
 //
 // Staging: in the fused step the seven input fields of a plane slot are
-// fetched by TMA (cp.async.bulk.tensor, one 34x10x1 box per field) into a
+// fetched by TMA (cp.async.bulk.tensor, one 18x18x1 box per field) into a
 // ring of three slots, two planes ahead of the plane being solved, each slot
 // completing on its own mbarrier.  Grids whose row pitch is not a multiple of
 // 16 bytes (odd n0) and the per-operator godunov (arbitrary caller pointers)
@@ -50,12 +52,7 @@ struct TileLayout {
     static constexpr int NFX = (TX + 1) * TY;
     static constexpr int NFY = TX * (TY + 1);
     static constexpr int NFZ = TX * TY;
-    // The face loop's index space: each face family starts on a warp
-    // boundary, so no warp splits its lanes between two families (a split
-    // warp runs the HLLC once per family, each time with part of its lanes).
-    static constexpr int NFX_W = (NFX + 31) / 32 * 32;
-    static constexpr int NFY_W = (NFY + 31) / 32 * 32;
-    static constexpr int NFACE_W = NFX_W + NFY_W + NFZ;
+    static constexpr int NFACE = NFX + NFY + NFZ;
     static constexpr int NT = TX * TY;
     // shared memory, in T elements after a 128-byte mbarrier block
     static constexpr int Q_ELEMS = NSLOT * kFields * PLANE_PAD;
@@ -193,12 +190,14 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
 template <class T, int PLANE_PAD>
 __device__ __forceinline__ Side<T> load_side(T const* q, int c, int dir)
 {
+    int const d1 = dir == 2 ? 0 : dir + 1; // the axes after the normal, cyclically
+    int const d2 = dir == 0 ? 2 : dir - 1;
     Side<T> s;
     s.d = q[0 * PLANE_PAD + c];
     s.p = q[1 * PLANE_PAD + c];
     s.un = q[(2 + dir) * PLANE_PAD + c];
-    s.ut1 = q[(2 + (dir + 1) % 3) * PLANE_PAD + c];
-    s.ut2 = q[(2 + (dir + 2) % 3) * PLANE_PAD + c];
+    s.ut1 = q[(2 + d1) * PLANE_PAD + c];
+    s.ut2 = q[(2 + d2) * PLANE_PAD + c];
     s.c = q[5 * PLANE_PAD + c];
     s.e = q[6 * PLANE_PAD + c];
     return s;
@@ -207,11 +206,13 @@ __device__ __forceinline__ Side<T> load_side(T const* q, int c, int dir)
 template <class T>
 __device__ __forceinline__ void store_flux(T* out, int stride, int idx, int dir, Flux<T> const& f)
 {
+    int const d1 = dir == 2 ? 0 : dir + 1;
+    int const d2 = dir == 0 ? 2 : dir - 1;
     out[0 * stride + idx] = f.d;
     out[1 * stride + idx] = f.e;
     out[(2 + dir) * stride + idx] = f.n;
-    out[(2 + (dir + 1) % 3) * stride + idx] = f.t1;
-    out[(2 + (dir + 2) % 3) * stride + idx] = f.t2;
+    out[(2 + d1) * stride + idx] = f.t1;
+    out[(2 + d2) * stride + idx] = f.t2;
 }
 
 // Per-CTA state of the tile engine that lives across work items.
@@ -331,34 +332,20 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
         // ---- face phase
         T const* qc = slot_field<T, TX, TY, NSLOT>(smem, cur, 0);
         T const* qn = slot_field<T, TX, TY, NSLOT>(smem, nxt, 0);
-        for (int f = tid; f < L::NFACE_W; f += L::NT) {
-            if (f < L::NFX_W) {
-                if (f < L::NFX) {
-                    int const fj = f / (TX + 1);
-                    int const fi = f % (TX + 1);
-                    int const a = (fj + 1) * L::HX + fi;
-                    store_flux(fx, L::NFX, f, 0,
-                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 0),
-                                         load_side<T, L::PLANE_PAD>(qc, a + 1, 0)));
-                }
-            } else if (f < L::NFX_W + L::NFY_W) {
-                int const g = f - L::NFX_W;
-                if (g < L::NFY) {
-                    int const fj = g / TX;
-                    int const fi = g % TX;
-                    int const a = fj * L::HX + fi + 1;
-                    store_flux(fy, L::NFY, g, 1,
-                               hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 1),
-                                         load_side<T, L::PLANE_PAD>(qc, a + L::HX, 1)));
-                }
-            } else {
-                int const g = f - L::NFX_W - L::NFY_W; // < NFZ
-                int const fj = g / TX;
-                int const fi = g % TX;
-                int const a = (fj + 1) * L::HX + fi + 1;
-                store_flux(fz, L::NFZ, g, 2,
-                           hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, 2), load_side<T, L::PLANE_PAD>(qn, a, 2)));
-            }
+        for (int f = tid; f < L::NFACE; f += L::NT) {
+            // the face's family, left cell and right cell, chosen by selects:
+            // a warp that straddles two families still runs the HLLC once
+            bool const is_x = f < L::NFX;
+            bool const is_y = !is_x && f < L::NFX + L::NFY;
+            int const g = is_x ? f : (is_y ? f - L::NFX : f - L::NFX - L::NFY);
+            int const gj = is_x ? g / (TX + 1) : g / TX;
+            int const gi = g - gj * (is_x ? TX + 1 : TX);
+            int const a = (is_y ? gj : gj + 1) * L::HX + (is_x ? gi : gi + 1);
+            int const dir = is_x ? 0 : (is_y ? 1 : 2);
+            T const* const qr = is_x || is_y ? qc : qn;
+            int const ar = a + (is_x ? 1 : (is_y ? L::HX : 0));
+            store_flux(is_x ? fx : (is_y ? fy : fz), is_x ? L::NFX : (is_y ? L::NFY : L::NFZ), g, dir,
+                       hllc_flux(load_side<T, L::PLANE_PAD>(qc, a, dir), load_side<T, L::PLANE_PAD>(qr, ar, dir)));
         }
         if (__syncthreads_or(c.timed_out)) {
             return false;
@@ -785,8 +772,11 @@ __global__ void finalize_batch_kernel(SimScalars* s, int ngrids, T cfl, int add_
     }
 }
 
-constexpr int kTX = 32;
-constexpr int kTY = 8;
+// The single-grid tile: 16x16 columns.  Its 800 faces per plane fill
+// exactly 25 warp-passes (a 32x8 tile's 808 need 26) with the same 256
+// threads, 18x18 TMA boxes and two resident CTAs per SM.
+constexpr int kTX = 16;
+constexpr int kTY = 16;
 
 
 template <class T, int MODE, bool TMA, int COMP>
