@@ -57,10 +57,10 @@ CFL = 0.4
 FLOPS_PER_CELL_DEFAULT = None
 
 # DRAM bytes (read + write) per interior cell of the fused FP64 kernel, from
-# one ncu capture at 192^3 (profiles/flux_step_f64_192.md: 672 MB + 582 MB over
+# one ncu capture at 192^3 (profiles/flux_step_f64_192.md: 674 MB + 580 MB over
 # 7.08 M interior cells); the kernel streams each plane once, so traffic
 # scales with cells.
-FLUX_F64_DRAM_BYTES_PER_CELL = 177.1
+FLUX_F64_DRAM_BYTES_PER_CELL = 177.3
 
 
 def parse():
@@ -694,7 +694,7 @@ def run_ours(args):
             "kernel": "flux_tile_kernel<double, step>", "kernel_ms": flux_ms,
             "step_ms_sum_of_launches": step_ms_launches,
             "traffic": FLUX_F64_DRAM_BYTES_PER_CELL * interior,
-            "traffic_note": "dram bytes read+write per launch: 177.1 B per interior cell from an ncu capture at "
+            "traffic_note": "dram bytes read+write per launch: 177.3 B per interior cell from an ncu capture at "
                             "192^3 (profiles/flux_step_f64_192.md), scaled by cells"}
     if fpc:
         fl = fpc["fused_step_fp64"] * interior
