@@ -20,13 +20,14 @@
 //              area ds, which the face kernel then need not apply.
 //   adj_face   per cell, its three upper faces: the HLLC solve recomputed
 //              from prim_n (nothing of the forward solve is stored), then
-//              its transpose applied to g = ds (w_R - w_L).  The cell keeps
-//              the sum of the three left halves (its own) and stores the
-//              right half of each face (the neighbour's) apart.
-//   adj_gather per cell: its own sum plus the right halves its three lower
-//              neighbours stored -- every cell reads only halves meant for
-//              it, so there are no atomics -- then the cons_to_prim or
-//              prim_to_cons transpose.
+//              its transpose applied to g = ds (w_R - w_L); each face's left
+//              half (the cell's share) and right half (the neighbour's) are
+//              stored apart.  Faces with a cotangent are queued per warp and
+//              solved 32 at a time.
+//   adj_gather per cell: the left halves of its three upper faces plus the
+//              right halves of its three lower neighbours' -- every cell
+//              reads only halves meant for it, so there are no atomics --
+//              then the cons_to_prim or prim_to_cons transpose.
 //
 // Ties.  The HLLC flux is piecewise smooth: it takes min/max of wave-speed
 // estimates and branches on the sign of ustar.  At an exact tie (equal
@@ -136,63 +137,106 @@ __device__ __forceinline__ FaceSide load_side(AdjParams const& p, long long c, i
     return s;
 }
 
-// The face halves a cell stores: its own sum over the left halves of its three
-// upper faces (index f), and the right half of each upper face (5 + a*5 + f),
-// which belongs to the neighbour c + e_a.
+// The transposed flux of the face between cell c and c + e_a, its two halves
+// stored apart: the left half (c's share) in face[a*5 + f][c], the right half
+// (the neighbour's share) in face[15 + a*5 + f][c].
+template <bool UNIT>
+__device__ __forceinline__ void face_task(AdjParams const& p, long long c, int a)
+{
+    int const b = a == 2 ? 0 : a + 1, e = a == 0 ? 2 : a - 1;
+    long long const cr = c + (a == 0 ? 1 : (a == 1 ? p.g.s1 : p.g.s2));
+    double dw[5];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+        dw[f] = p.w.weight[f][cr] - p.w.weight[f][c];
+    }
+    FaceSide const L = load_side(p, c, a);
+    FaceSide const R = load_side(p, cr, a);
+    FaceBar bL, bR;
+    hllc_bar<UNIT>(L, R, dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], p.ds[a], p.inv_gm1, bL, bR);
+    double* const* hl = p.w.face + a * 5;
+    double* const* hr = p.w.face + 15 + a * 5;
+    hl[0][c] = bL.r;
+    hl[1][c] = bL.p;
+    hl[2 + a][c] = bL.un;
+    hl[2 + b][c] = bL.t1;
+    hl[2 + e][c] = bL.t2;
+    hr[0][c] = bR.r;
+    hr[1][c] = bR.p;
+    hr[2 + a][c] = bR.un;
+    hr[2 + b][c] = bR.t1;
+    hr[2 + e][c] = bR.t2;
+}
+
+// Each cell's three upper faces.  The faces that carry a cotangent are not
+// solved where they are found: a warp queues them in shared memory and runs
+// the transposed flux 32 at a time, so every lane of the FP64 work is busy.
+// (Faces outside the cotangent's support -- the functional's region grown by
+// one cell per reverse step, and wherever the two cells' weights are equal --
+// are interleaved with the others at the lane level; solved in place they
+// left a quarter of the FP64 lanes idle.)  A face without work gets zero
+// halves.  The test for work compares the two cells' weight bits on the
+// integer pipe: equal finite weights give w_R - w_L == 0 in every field.
 template <bool UNIT>
 __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
 {
+    __shared__ long long queue[kThreads / 32][64]; // queued faces: cell * 4 + axis
     long long const n = p.g.ncell();
-    long long const stride[3] = {1, p.g.s1, p.g.s2};
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
-         c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        int idx[3];
-        decode(p.g, c, idx[0], idx[1], idx[2]);
-        int const ext[3] = {p.g.n0, p.g.n1, p.g.n2};
-        double self[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    int const lane = threadIdx.x & 31;
+    unsigned const below = (1u << lane) - 1u;
+    long long* const q = queue[threadIdx.x >> 5];
+    int qn = 0; // faces queued in this warp (the same in every lane)
+    int const ext[3] = {p.g.n0, p.g.n1, p.g.n2};
+    long long const stride = static_cast<long long>(gridDim.x) * blockDim.x;
+    // warp-uniform trip count: every lane of a warp runs every iteration
+    for (long long base = blockIdx.x * static_cast<long long>(blockDim.x) + (threadIdx.x & ~31); base < n;
+         base += stride) {
+        long long const c = base + lane;
+        bool const valid = c < n;
+        int idx[3] = {0, 0, 0};
+        if (valid) {
+            decode(p.g, c, idx[0], idx[1], idx[2]);
+        }
 #pragma unroll 1
         for (int a = 0; a < 3; ++a) {
-            int const b = (a + 1) % 3, e = (a + 2) % 3;
+            int const b = a == 2 ? 0 : a + 1, e = a == 0 ? 2 : a - 1;
             // the face between c and c + e_a is solved by the step when one side is interior
-            bool const active = idx[a] <= ext[a] - 2 && idx[b] >= 1 && idx[b] <= ext[b] - 2 && idx[e] >= 1 &&
-                                idx[e] <= ext[e] - 2;
-            FaceBar bL, bR;
-            zero(bL);
-            zero(bR);
+            bool const active = valid && idx[a] <= ext[a] - 2 && idx[b] >= 1 && idx[b] <= ext[b] - 2 &&
+                                idx[e] >= 1 && idx[e] <= ext[e] - 2;
+            bool need = false;
             if (active) {
-                long long const cr = c + stride[a];
-                double dw[5];
-                bool any = false;
+                long long const cr = c + (a == 0 ? 1 : (a == 1 ? p.g.s1 : p.g.s2));
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    dw[f] = p.w.weight[f][cr] - p.w.weight[f][c];
-                    any = any || !adj_zero(dw[f]); // on the integer pipe
-                }
-                // a face outside the cotangent's support contributes nothing (early reverse
-                // steps: the support is the functional's region grown by one cell per step)
-                if (any) {
-                    FaceSide const L = load_side(p, c, a);
-                    FaceSide const R = load_side(p, cr, a);
-                    hllc_bar<UNIT>(L, R, dw[0], dw[1], dw[2 + a], dw[2 + b], dw[2 + e], p.ds[a], p.inv_gm1, bL,
-                                   bR);
+                    long long const wl = adj_bits(p.w.weight[f][c]);
+                    long long const wr = adj_bits(p.w.weight[f][cr]);
+                    need = need || wl != wr || (wl & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
                 }
             }
-            self[0] += bL.r;
-            self[1] += bL.p;
-            self[2 + a] += bL.un;
-            self[2 + b] += bL.t1;
-            self[2 + e] += bL.t2;
-            double* const* fr = p.w.face + 5 + a * 5;
-            fr[0][c] = bR.r;
-            fr[1][c] = bR.p;
-            fr[2 + a][c] = bR.un;
-            fr[2 + b][c] = bR.t1;
-            fr[2 + e][c] = bR.t2;
-        }
+            if (valid && !need) {
 #pragma unroll
-        for (int f = 0; f < 5; ++f) {
-            p.w.face[f][c] = self[f];
+                for (int f = 0; f < 5; ++f) {
+                    p.w.face[a * 5 + f][c] = 0.0;
+                    p.w.face[15 + a * 5 + f][c] = 0.0;
+                }
+            }
+            unsigned const m = __ballot_sync(0xffffffffu, need);
+            if (need) {
+                q[qn + __popc(m & below)] = c * 4 + a;
+            }
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                long long const t = q[qn - 32 + lane];
+                __syncwarp(); // every lane has its task before the slots are refilled
+                qn -= 32;
+                face_task<UNIT>(p, t >> 2, static_cast<int>(t & 3));
+            }
         }
+    }
+    if (lane < qn) {
+        long long const t = q[lane];
+        face_task<UNIT>(p, t >> 2, static_cast<int>(t & 3));
     }
 }
 
@@ -210,11 +254,12 @@ __global__ void __launch_bounds__(kThreads) adj_gather_kernel(AdjParams p, CBund
         double pb[5];
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
-            double s = p.w.face[f][c]; // faces where this cell is the left side
+            // the three faces where this cell is the left side ...
+            double s = p.w.face[f][c] + p.w.face[5 + f][c] + p.w.face[10 + f][c];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 if (idx[a] >= 1) {
-                    s += p.w.face[5 + a * 5 + f][c - stride[a]]; // ... and the right side
+                    s += p.w.face[15 + a * 5 + f][c - stride[a]]; // ... and the three where it is the right
                 }
             }
             pb[f] = s;
@@ -326,7 +371,7 @@ AdjWork adjoint_workspace(void* base, long long ncell)
     AdjWork w{};
     size_t const field = pad_field(ncell);
     char* p = static_cast<char*>(base);
-    for (int f = 0; f < 20; ++f, p += field) {
+    for (int f = 0; f < 30; ++f, p += field) {
         w.face[f] = reinterpret_cast<double*>(p);
     }
     for (int f = 0; f < 6; ++f, p += field) {

@@ -151,13 +151,14 @@ cudaError_t launch_state_from_f32(CBundle<float> hi, CBundle<float> lo, Bundle<d
 constexpr int kAdjStep = 0;    // out = dJ/dcons: cbar + cons_to_prim'(prim)^T pbar
 constexpr int kAdjInitial = 1; // out = dJ/dprim of a step that reads prim itself: pbar + prim_to_cons'(prim)^T cbar
 constexpr int kAdjGodunov = 2; // out = pbar = (d godunov / d prim)^T cbar
-constexpr int kAdjWorkFields = 31;
+constexpr int kAdjWorkFields = 41;
 
-// Workspace of the reverse step: per cell, the sum of the left halves of its
-// three upper faces (index prim field) and the right half of each (5 + axis*5
-// + prim field); sound speed data and energies; the weighted cotangent.
+// Workspace of the reverse step: per cell and per upper face (axis a), the
+// face's left half (a*5 + prim field) and its right half (15 + a*5 + prim
+// field), which belongs to the neighbour c + e_a; sound speed data and
+// energies; the weighted cotangent.
 struct AdjWork {
-    double* face[20];
+    double* face[30];
     double* derived[6]; // c, dc/dp, dc/drho, total energy, kinetic energy per mass, 1/rho
     double* weight[5];  // (dt/dv) cbar on interior cells, 0 on ghosts
 };

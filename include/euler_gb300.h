@@ -334,7 +334,7 @@ int eulr_batch_info(eulr_batch* batch, long long* interior_cells, int* nitems, i
  * central difference measures.  All pointers are device memory. */
 
 /* Bytes of device workspace eulr_godunov_adjoint_f64 needs for a grid
- * (31 FP64 fields of n0*n1*n2 values, each padded to 256 bytes); 0 when the
+ * (41 FP64 fields of n0*n1*n2 values, each padded to 256 bytes); 0 when the
  * extents are invalid. */
 size_t eulr_godunov_adjoint_workspace_bytes(int n0, int n1, int n2);
 
