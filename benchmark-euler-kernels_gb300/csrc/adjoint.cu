@@ -170,22 +170,27 @@ __device__ __forceinline__ void face_task(AdjParams const& p, long long c, int a
 
 // Each cell's three upper faces.  The faces that carry a cotangent are not
 // solved where they are found: a warp queues them in shared memory and runs
-// the transposed flux 32 at a time, so every lane of the FP64 work is busy.
+// the transposed flux 32 at a time, so no lane idles for want of a face.
 // (Faces outside the cotangent's support -- the functional's region grown by
 // one cell per reverse step, and wherever the two cells' weights are equal --
 // are interleaved with the others at the lane level; solved in place they
-// left a quarter of the FP64 lanes idle.)  A face without work gets zero
-// halves.  The test for work compares the two cells' weight bits on the
+// left a quarter of the FP64 lanes idle.)  Two queues keep the two paths of
+// the transposed flux apart: faces of gas at rest with equal pressures on
+// both sides (both normal velocities +-0, equal pressure bits: every term of
+// num is a signed zero, so ustar == 0 exactly and the tie path runs) and all
+// the others; mixed in one warp they cost a further 15 % of the lanes.  A
+// tie found any other way still takes its own path, inside the second
+// queue.  A face without work gets zero halves.  The tests run on the
 // integer pipe: equal finite weights give w_R - w_L == 0 in every field.
 template <bool UNIT>
 __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
 {
-    __shared__ long long queue[kThreads / 32][64]; // queued faces: cell * 4 + axis
+    __shared__ long long queue[kThreads / 32][2][64]; // queued faces: cell * 4 + axis
     long long const n = p.g.ncell();
     int const lane = threadIdx.x & 31;
     unsigned const below = (1u << lane) - 1u;
-    long long* const q = queue[threadIdx.x >> 5];
-    int qn = 0; // faces queued in this warp (the same in every lane)
+    long long(*const q)[64] = queue[threadIdx.x >> 5];
+    int qn[2] = {0, 0}; // faces queued in this warp, per queue (the same in every lane)
     int const ext[3] = {p.g.n0, p.g.n1, p.g.n2};
     long long const stride = static_cast<long long>(gridDim.x) * blockDim.x;
     // warp-uniform trip count: every lane of a warp runs every iteration
@@ -204,6 +209,7 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
             bool const active = valid && idx[a] <= ext[a] - 2 && idx[b] >= 1 && idx[b] <= ext[b] - 2 &&
                                 idx[e] >= 1 && idx[e] <= ext[e] - 2;
             bool need = false;
+            bool quiet = false;
             if (active) {
                 long long const cr = c + (a == 0 ? 1 : (a == 1 ? p.g.s1 : p.g.s2));
 #pragma unroll
@@ -212,6 +218,8 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
                     long long const wr = adj_bits(p.w.weight[f][cr]);
                     need = need || wl != wr || (wl & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
                 }
+                quiet = adj_zero(p.prim.f[2 + a][c]) && adj_zero(p.prim.f[2 + a][cr]) &&
+                        adj_bits(p.prim.f[1][c]) == adj_bits(p.prim.f[1][cr]);
             }
             if (valid && !need) {
 #pragma unroll
@@ -220,23 +228,33 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
                     p.w.face[15 + a * 5 + f][c] = 0.0;
                 }
             }
-            unsigned const m = __ballot_sync(0xffffffffu, need);
-            if (need) {
-                q[qn + __popc(m & below)] = c * 4 + a;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                bool const mine = need && (quiet == (k == 1));
+                unsigned const m = __ballot_sync(0xffffffffu, mine);
+                if (mine) {
+                    q[k][qn[k] + __popc(m & below)] = c * 4 + a;
+                }
+                qn[k] += __popc(m);
             }
-            qn += __popc(m);
             __syncwarp();
-            if (qn >= 32) {
-                long long const t = q[qn - 32 + lane];
-                __syncwarp(); // every lane has its task before the slots are refilled
-                qn -= 32;
-                face_task<UNIT>(p, t >> 2, static_cast<int>(t & 3));
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (qn[k] >= 32) {
+                    long long const t = q[k][qn[k] - 32 + lane];
+                    __syncwarp(); // every lane has its task before the slots are refilled
+                    qn[k] -= 32;
+                    face_task<UNIT>(p, t >> 2, static_cast<int>(t & 3));
+                }
             }
         }
     }
-    if (lane < qn) {
-        long long const t = q[lane];
-        face_task<UNIT>(p, t >> 2, static_cast<int>(t & 3));
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (lane < qn[k]) {
+            long long const t = q[k][lane];
+            face_task<UNIT>(p, t >> 2, static_cast<int>(t & 3));
+        }
     }
 }
 
