@@ -752,6 +752,19 @@ def run_ours(args):
         outs = [torch.empty((5, n0, n0, n0), dtype=torch.float64, pin_memory=True) for _ in range(nsim)]
         src = random_prim_device(torch, n0, n0, n0, seed=2)
         host.copy_(src)
+        torch.cuda.synchronize()
+        # the host link this run sees: it differs between machines, with the
+        # host's other traffic, and it bounds the copies of every step
+        link = {}
+        for name, fn in (("h2d", lambda: src.copy_(host, non_blocking=True)),
+                         ("d2h", lambda: host.copy_(src, non_blocking=True))):
+            fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(2):
+                fn()
+            torch.cuda.synchronize()
+            link[name] = 2 * host.numel() * 8 / (time.perf_counter() - t0) / 1e9
         del src
         torch.cuda.synchronize()
         streams = [torch.cuda.Stream() for _ in range(nsim)]
@@ -762,6 +775,8 @@ def run_ours(args):
             sm.get_state(prim=outs[q])
         torch.cuda.synchronize()
         runs = []
+        e2e_clocks = ClockSampler(local)
+        e2e_clocks.start()
         for _ in range(3):  # host-link bandwidth varies with the machine's other tenants: median of 3
             t0 = time.perf_counter()
             for step in range(args.e2e_steps):
@@ -775,11 +790,13 @@ def run_ours(args):
             for sm in sims:
                 sm.synchronize()
             runs.append(world * interior * args.e2e_steps / (time.perf_counter() - t0) / 1e9)
+        e2e_clk = e2e_clocks.stop()
         for sm in sims:
             sm.close()
         nbytes = 5 * n0 ** 3 * 8
         e2e = {"value": sorted(runs)[1], "unit": UNIT, "runs": runs,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
+               "link_gbs": link, "clocks": e2e_clk,
                "how": "per step: eulr_sim_set_prim_f64 from pinned host prim (H2D, then prim_to_cons, sound speed "
                       "and first dt in one kernel), eulr_sim_advance(1), eulr_sim_get_state_async_f64 of prim to "
                       "pinned host (D2H); three simulations on three streams take the steps in turn so copies "
