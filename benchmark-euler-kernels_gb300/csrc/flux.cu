@@ -9,12 +9,14 @@
 // (TX+2) x (TY+2) plane with its one-cell halo.  Per plane:
 //   1. face phase -- every x face and y face of plane k and every z face
 //      between planes k and k+1 is solved ONCE (the reference solves each
-//      interior face twice, once from each side, godunov.hpp:48-82).  The
-//      x, y and z faces share one index space, and each face's family,
-//      cells and axis permutation are chosen by selects, so a warp whose
-//      lanes straddle two families still runs the HLLC once: the 800 faces
-//      of a 16x16 tile take exactly 25 warp-passes.  Fluxes go to shared
-//      memory in global axes;
+//      interior face twice, once from each side, godunov.hpp:48-82).  FP64
+//      (bound by the FP64 pipe): the x, y and z faces share one index space,
+//      and each face's family, cells and axis permutation are chosen by
+//      selects, so a warp whose lanes straddle two families still runs the
+//      HLLC once -- the 800 faces of a 16x16 tile take exactly 25
+//      warp-passes.  FP32 (bound by instruction issue): each family in its
+//      own warp-aligned range with compile-time axes, on a 32x8 tile.
+//      Fluxes go to shared memory in global axes;
 //   2. cell phase -- each thread owns one column cell and applies
 //      cons -= dt/dv * sum_d ds_d (F_R - F_L) (godunov.hpp:84-90) with the
 //      face-area and dt/dv factors folded into three coefficients.  The z
@@ -24,7 +26,7 @@
 // atomicMax per CTA, so dt never leaves the device.
 //
 // Staging: in the fused step the seven input fields of a plane slot are
-// fetched by TMA (cp.async.bulk.tensor, one 18x18x1 box per field) into a
+// fetched by TMA (cp.async.bulk.tensor, one 18x18x1 FP64 box per field) into a
 // ring of three slots, two planes ahead of the plane being solved, each slot
 // completing on its own mbarrier.  Grids whose row pitch is not a multiple of
 // 16 bytes (odd n0) and the per-operator godunov (arbitrary caller pointers)
