@@ -115,13 +115,14 @@ def test_time_step_edge_values(cuda, euler, oracle_lib):
     assert got == ref
 
 
-@pytest.mark.parametrize("case", ["near_ties", "wide_range", "large_random"])
+@pytest.mark.parametrize("case", ["near_ties", "misordered", "wide_range", "large_random"])
 def test_time_step_screened_max_is_exact(cuda, euler, oracle_lib, case):
     """time_step and a simulation's first dt evaluate the exact wavespeed
     only where an FP32 estimate says it can be the max; dt stays the
     reference's bit for bit on states built against that screen: wavespeeds
-    a few ulps apart everywhere, values far outside FP32's range (always
-    evaluated exactly), and a large grid."""
+    a few ulps apart everywhere, cells whose estimates order them wrongly,
+    values far outside FP32's range (always evaluated exactly), and a large
+    grid."""
     O = oracle_lib
     rng = np.random.default_rng(31)
     if case == "near_ties":
@@ -130,6 +131,17 @@ def test_time_step_screened_max_is_exact(cuda, euler, oracle_lib, case):
         prim[0] = 1.0 + rng.integers(-8, 9, prim.shape[1:]) * 2.0 ** -52
         prim[1] = 1.0 + rng.integers(-8, 9, prim.shape[1:]) * 2.0 ** -52
         prim[2:] = 0.3
+    elif case == "misordered":
+        # the larger exact wavespeed behind the lower FP32 estimate: p 2^-45
+        # lower (truncated away) and u0 2^-30 higher (also truncated away)
+        shape = (40, 37, 33)
+        prim = np.empty((5,) + shape[::-1])
+        prim[0] = 1.0
+        prim[1] = 1.0 + 2.0 ** -20
+        prim[2:] = 0.25
+        planted = rng.choice(prim[0].size, 16, replace=False)
+        prim[1].reshape(-1)[planted] -= 2.0 ** -45
+        prim[2].reshape(-1)[planted] += 2.0 ** -30
     elif case == "wide_range":
         shape = (31, 29, 27)
         prim = O.random_prim(*shape, seed=5)
