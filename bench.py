@@ -451,7 +451,7 @@ def run_adjoint_leg(torch, E, stream, args, ndirs):
     wall = time.perf_counter() - t0
     tm = adj.timing()
     J = float((out[0] * w).sum())
-    rec = {"workload": f"init_implode {nx}^3 + rho noise N(0,1e-6), {nsteps} steps at fixed CFL dts, "
+    rec = {"workload": f"init_implode {nx}^3 + rho noise N(0, (1e-3)^2), {nsteps} steps at fixed CFL dts, "
                        f"checkpoints every {every}; J = sum over [0.4,0.6]^3 of rho(T) dv",
            "J": J, "t_final": float(sum(dts)),
            "forward_step_ms": fwd_step_ms,
