@@ -61,12 +61,15 @@ def test_implode_100_steps_time_and_totals(cuda, euler, oracle_lib):
         assert abs(tot[f] - ref_tot[f]) <= 1e-10 * abs(tot0[0])
 
 
-def test_random_state_steps(cuda, euler, oracle_lib):
-    """Seeded random states (rho, p log-uniform [0.1,10], u ~ N(0,1)) on a
-    ragged grid: 1 and 5 steps."""
+@pytest.mark.parametrize("shape", [(45, 38, 29), (46, 39, 30)], ids=["odd_n0_plain_loads", "even_n0_tma"])
+def test_random_state_steps(cuda, euler, oracle_lib, shape):
+    """Seeded random states (rho, p log-uniform [0.1,10], u ~ N(0,1)) on
+    ragged grids, 1 and 5 steps: partial tiles at the high edges, staged with
+    plain loads (odd n0: rows not a multiple of 16 bytes) and with TMA (even
+    n0: the boxes of the edge tiles reach past the array)."""
     O = oracle_lib
-    n0, n1, n2 = 45, 38, 29
-    dx = (1 / 43, 1 / 36, 1 / 27)
+    n0, n1, n2 = shape
+    dx = (1 / (n0 - 2), 1 / (n1 - 2), 1 / (n2 - 2))
     prim0 = O.random_prim(n0, n1, n2, seed=21)
     for steps, tol in ((1, TOL_1), (5, 1e-11)):
         p = prim0.copy()
