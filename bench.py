@@ -598,12 +598,18 @@ def time_ops(torch, E, prim, n_int, fpc=None, fp64_peak=None, hbm_peak=None):
     ms = timed(lambda: E.godunov(prim, cons, GAMMA, dx, 1e-9))
     out["godunov"] = {"ms": ms, "gcells_s": cells / ms / 1e6, "gb_s": 120 * cells / ms / 1e6,
                       "interior_gcells_s": interior / ms / 1e6}
+    ms = timed(lambda: E.godunov(prim, cons, GAMMA, dx, 1e-9, exact=True), reps=1)
+    out["godunov_exact"] = {"ms": ms, "gcells_s": cells / ms / 1e6, "gb_s": 120 * cells / ms / 1e6,
+                            "interior_gcells_s": interior / ms / 1e6,
+                            "note": "eulr_godunov_exact_f64: bit-identical to the reference (its operation order, "
+                                    "every operation rounded separately, each face solved by both of its cells)"}
     del cons, prim2
     if fpc:
         flops = {"prim_to_cons": (fpc["prim_to_cons_per_cell"]["total"], cells),
                  "cons_to_prim": (fpc["cons_to_prim_per_cell"]["total"], cells),
                  "time_step": (fpc["time_step_per_cell"]["total"], cells),
-                 "godunov": (3 * fpc["hllc_face"]["total"] + fpc["godunov_update_per_cell"]["total"], interior)}
+                 "godunov": (3 * fpc["hllc_face"]["total"] + fpc["godunov_update_per_cell"]["total"], interior),
+                 "godunov_exact": (fpc["godunov_reference_per_cell"]["total"], interior)}
         for name, (per_cell, units) in flops.items():
             rec = out[name]
             rec["flops_per_cell"] = per_cell
@@ -613,7 +619,7 @@ def time_ops(torch, E, prim, n_int, fpc=None, fp64_peak=None, hbm_peak=None):
             if hbm_peak:
                 rec["hbm_frac"] = rec["gb_s"] / hbm_peak
     # the roofline that bounds each operator on GB300 (profiles/pointwise_ops_f64_256.md)
-    for name in ("prim_to_cons", "cons_to_prim", "godunov"):
+    for name in ("prim_to_cons", "cons_to_prim", "godunov", "godunov_exact"):
         out[name]["bound"] = "fp64"
     out["time_step"]["bound"] = "hbm"
     out["time_step"]["note"] = ("the max wavespeed is screened by an FP32 estimate built on the integer and FP32 "

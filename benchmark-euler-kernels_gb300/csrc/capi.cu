@@ -280,7 +280,7 @@ int time_step_impl(PB prim, int n0, int n1, int n2, T gamma, T dx0, T dx1, T dx2
 
 template <class T, class PB, class CB>
 int godunov_impl(PB prim, CB cons, int n0, int n1, int n2, T gamma, T dx0, T dx1, T dx2, T dt, const T* dt_dev,
-                 T cfl, cudaStream_t s)
+                 T cfl, cudaStream_t s, bool exact = false)
 {
     EULR_TRY(check_dims(n0, n1, n2));
     EULR_TRY(check_fields<T>(reinterpret_cast<const void* const*>(&prim), 5, "prim"));
@@ -299,6 +299,12 @@ int godunov_impl(PB prim, CB cons, int n0, int n1, int n2, T gamma, T dx0, T dx1
     EULR_TRY(check_disjoint(all, 10, static_cast<size_t>(n0) * n1 * n2 * sizeof(T), "godunov"));
     int sms = 0;
     EULR_TRY(current_sms(&sms));
+    if (exact) {
+        EULR_CUDA_TRY(launch_godunov_exact<T>(to_cbundle<T>(prim), to_bundle<T>(cons), make_geom(n0, n1, n2), gamma,
+                                              dx0, dx1, dx2, dt, sms, s),
+                      "godunov (exact) launch");
+        return EULR_SUCCESS;
+    }
     FluxParams<T> p{};
     p.g = make_geom(n0, n1, n2);
     p.prim = to_cbundle<T>(prim);
@@ -465,6 +471,18 @@ int eulr_godunov_f32(eulr_prim_cf32 prim, eulr_cons_f32 cons, int n0, int n1, in
                      float dx1, float dx2, float dt, eulr_stream_t stream)
 {
     return godunov_impl<float>(prim, cons, n0, n1, n2, gamma, dx0, dx1, dx2, dt, nullptr, 0.0f, stream);
+}
+
+int eulr_godunov_exact_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int n1, int n2, double gamma, double dx0,
+                           double dx1, double dx2, double dt, eulr_stream_t stream)
+{
+    return godunov_impl<double>(prim, cons, n0, n1, n2, gamma, dx0, dx1, dx2, dt, nullptr, 0.0, stream, true);
+}
+
+int eulr_godunov_exact_f32(eulr_prim_cf32 prim, eulr_cons_f32 cons, int n0, int n1, int n2, float gamma, float dx0,
+                           float dx1, float dx2, float dt, eulr_stream_t stream)
+{
+    return godunov_impl<float>(prim, cons, n0, n1, n2, gamma, dx0, dx1, dx2, dt, nullptr, 0.0f, stream, true);
 }
 
 int eulr_godunov_devdt_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int n1, int n2, double gamma,

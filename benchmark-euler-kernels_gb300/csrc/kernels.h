@@ -114,6 +114,10 @@ cudaError_t configure_flux(int mode, bool tma, int comp, int* per_sm);
 // maps != nullptr selects TMA staging (step mode only); comp: kComp* (float step mode)
 template <class T>
 cudaError_t launch_flux(FluxParams<T> p, TmaMaps const* maps, int mode, int comp, int sms, cudaStream_t s);
+// godunov bit-identical to the reference (godunov_exact.cu); cons updated in place.
+template <class T>
+cudaError_t launch_godunov_exact(CBundle<T> prim, Bundle<T> cons, Geom g, T gamma, T dx0, T dx1, T dx2, T dt, int sms,
+                                 cudaStream_t s);
 int flux_tile_x();
 int flux_tile_y();
 

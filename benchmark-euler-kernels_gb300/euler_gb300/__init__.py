@@ -65,6 +65,8 @@ _SIGNATURES = [
     ("eulr_godunov_f64", _I, [Bundle5, Bundle5, _I, _I, _I, _D, _D, _D, _D, _D, _P]),
     ("eulr_godunov_f32", _I, [Bundle5, Bundle5, _I, _I, _I, _F, _F, _F, _F, _F, _P]),
     ("eulr_godunov_devdt_f64", _I, [Bundle5, Bundle5, _I, _I, _I, _D, _D, _D, _D, _P, _D, _P]),
+    ("eulr_godunov_exact_f64", _I, [Bundle5, Bundle5, _I, _I, _I, _D, _D, _D, _D, _D, _P]),
+    ("eulr_godunov_exact_f32", _I, [Bundle5, Bundle5, _I, _I, _I, _F, _F, _F, _F, _F, _P]),
     ("eulr_sim_create", _I, [_I, _I, _I, _I, _D, _D, _D, _D, _D, _P, ctypes.POINTER(_P)]),
     ("eulr_sim_destroy", _I, [_P]),
     ("eulr_sim_set_prim_f64", _I, [_P, Bundle5]),
@@ -222,12 +224,19 @@ def time_step(prim, gamma, dx, out=None, stream=None):
     return dt
 
 
-def godunov(prim, cons, gamma, dx, dt, stream=None):
+def godunov(prim, cons, gamma, dx, dt, stream=None, exact=False):
     """In-place update of cons (interior cells) from prim; dt is a float or a
     device scalar tensor (then dt_used = cfl * dt with cfl given as a tuple
-    (tensor, cfl))."""
+    (tensor, cfl)).  exact=True: bit-identical to the reference
+    (eulr_godunov_exact_*; a float dt only)."""
     sfx = _sfx(prim)
     c = _scalar(sfx)
+    if exact:
+        if isinstance(dt, tuple):
+            raise ValueError("the exact godunov takes dt as a number")
+        check(getattr(load(), f"eulr_godunov_exact_{sfx}")(bundle(prim), bundle(cons), *dims(prim), c(gamma),
+                                                            c(dx[0]), c(dx[1]), c(dx[2]), c(dt), _stream(stream)))
+        return cons
     if isinstance(dt, tuple):
         dt_t, cfl = dt
         check(load().eulr_godunov_devdt_f64(bundle(prim), bundle(cons), *dims(prim), c(gamma), c(dx[0]),

@@ -4,8 +4,10 @@
 // read-only prim, cons updated in place.  Runs on the GPU through
 // eulr_godunov_{f64,f32}, which solves each face once (the reference solves
 // each interior face from both sides); results agree with the reference
-// within 1e-12 relative L-infinity in FP64.  Enqueued on the execution
-// space's stream; returns without waiting.
+// within 1e-12 relative L-infinity in FP64.  Defining EULR_GODUNOV_BIT_EXACT
+// before including this header routes it to eulr_godunov_exact_{f64,f32}
+// instead: the reference's results bit for bit, about four times slower.
+// Enqueued on the execution space's stream; returns without waiting.
 #pragma once
 
 #include <euler_arrays.hpp>
@@ -32,14 +34,21 @@ void godunov(
     using ty = b::types<T>;
     auto const& s = prim_arrays.d;
     int st;
+#ifdef EULR_GODUNOV_BIT_EXACT
+    auto* const f64 = &eulr_godunov_exact_f64;
+    auto* const f32 = &eulr_godunov_exact_f32;
+#else
+    auto* const f64 = &eulr_godunov_f64;
+    auto* const f32 = &eulr_godunov_f32;
+#endif
     if constexpr (std::is_same_v<T, double>) {
-        st = eulr_godunov_f64(b::prim_ptrs<typename ty::cprim>(prim_arrays), b::cons_ptrs<typename ty::cons>(cons_arrays),
-                              b::extent_int(s, 0), b::extent_int(s, 1), b::extent_int(s, 2), eos.gamma(), mesh.dx0(),
-                              mesh.dx1(), mesh.dx2(), dt, b::stream_of(exec_space));
+        st = f64(b::prim_ptrs<typename ty::cprim>(prim_arrays), b::cons_ptrs<typename ty::cons>(cons_arrays),
+                 b::extent_int(s, 0), b::extent_int(s, 1), b::extent_int(s, 2), eos.gamma(), mesh.dx0(), mesh.dx1(),
+                 mesh.dx2(), dt, b::stream_of(exec_space));
     } else {
-        st = eulr_godunov_f32(b::prim_ptrs<typename ty::cprim>(prim_arrays), b::cons_ptrs<typename ty::cons>(cons_arrays),
-                              b::extent_int(s, 0), b::extent_int(s, 1), b::extent_int(s, 2), eos.gamma(), mesh.dx0(),
-                              mesh.dx1(), mesh.dx2(), dt, b::stream_of(exec_space));
+        st = f32(b::prim_ptrs<typename ty::cprim>(prim_arrays), b::cons_ptrs<typename ty::cons>(cons_arrays),
+                 b::extent_int(s, 0), b::extent_int(s, 1), b::extent_int(s, 2), eos.gamma(), mesh.dx0(), mesh.dx1(),
+                 mesh.dx2(), dt, b::stream_of(exec_space));
     }
     b::check(st, "godunov");
 }

@@ -36,10 +36,12 @@ def test_reference_driver_builds_against_dropin(euler, tmp_path):
     assert exe.exists()
 
 
-def test_reference_style_calls_compile_against_dropin(euler, tmp_path):
+@pytest.mark.parametrize("defines", [[], ["-DEULR_GODUNOV_BIT_EXACT"]], ids=["default", "bit_exact_godunov"])
+def test_reference_style_calls_compile_against_dropin(euler, tmp_path, defines):
     """The reference's operator call sequence (simulations/euler_simulation.cpp:
     37-67, benchmarks/benchmark_*.cpp) written against the drop-in: every type
-    and operator it names is provided."""
+    and operator it names is provided, with godunov on the default or the
+    bit-exact entry point."""
     _need_ref()
     src = tmp_path / "probe.cpp"
     src.write_text(
@@ -58,6 +60,6 @@ def test_reference_style_calls_compile_against_dropin(euler, tmp_path):
         "  cons_to_prim(exec_space, as_const(c), p, eos); exec_space.fence();\n"
         "  (void)size_bytes(p); (void)size(c); (void)load(p, 1, 1, 1);\n"
         "}\n")
-    r = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", *[f"-I{d}" for d in INC], str(src)],
+    r = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", *defines, *[f"-I{d}" for d in INC], str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]

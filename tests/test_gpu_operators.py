@@ -82,6 +82,38 @@ def test_random_operators_vs_oracle(cuda, euler, oracle_lib, shape):
     assert max(errs) <= TOL_F64_STEP, errs
 
 
+@pytest.mark.parametrize("path", OPS, ids=os.path.basename)
+def test_exact_godunov_matches_reference_fixtures(cuda, euler, path):
+    """The exact godunov against the fixtures made by the reference build
+    itself: every bit, f64 and f32, interior updated, ghosts untouched.  The
+    scalars are passed as the fixture generator passed them (gamma 1.4, its
+    CFL 0.4 times the fixture's dt)."""
+    z = np.load(path)
+    dx = tuple(float(v) for v in z["dx"])
+    cg = _t(cuda, z["cons"])
+    euler.godunov(_t(cuda, z["prim"]), cg, 1.4, dx, 0.4 * float(z["dt"][()]), exact=True)
+    assert np.array_equal(cg.cpu().numpy(), z["cons_godunov"])
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("shape,dx", [((70, 40, 37), (0.02, 0.03, 0.05)), ((33, 34, 35), (0.1, 0.1, 0.1)),
+                                      ((3, 3, 3), (1.0, 1.0, 1.0)), ((2, 9, 9), (0.5, 0.25, 0.125))])
+def test_exact_godunov_bit_identical_to_oracle(cuda, euler, oracle_lib, dtype, shape, dx):
+    """The exact godunov equals the oracle's, itself bit-identical to the
+    reference build, on seeded random states (including supersonic faces),
+    ragged, tiny and degenerate grids."""
+    O = oracle_lib
+    prim = O.random_prim(*shape, seed=sum(shape))
+    if dtype == "f32":
+        prim = prim.astype(np.float32)
+    cons = O.prim_to_cons(prim, 1.4)
+    dt = 0.4 * O.time_step(prim, 1.4, dx)
+    ref = O.godunov(prim, cons, 1.4, dx, dt)
+    cg = _t(cuda, cons)
+    euler.godunov(_t(cuda, prim), cg, 1.4, dx, dt, exact=True)
+    assert np.array_equal(cg.cpu().numpy(), ref)
+
+
 def test_godunov_device_dt_matches_host_dt(cuda, euler, oracle_lib):
     O = oracle_lib
     prim = O.random_prim(40, 33, 20, seed=4)
