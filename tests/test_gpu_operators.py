@@ -114,6 +114,35 @@ def test_exact_godunov_bit_identical_to_oracle(cuda, euler, oracle_lib, dtype, s
     assert np.array_equal(cg.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("init", ["implode", "random"])
+def test_reference_loop_bit_identical(cuda, euler, oracle_lib, dtype, init):
+    """The reference's time loop (simulations/euler_simulation.cpp:56-68:
+    time_step -> godunov(cfl*dt) -> cons_to_prim, with cfl*dt formed in T) run
+    on the GPU through the bit-identical operators -- time_step, the exact
+    godunov, cons_to_prim -- equals the oracle's loop bit for bit after 20
+    steps."""
+    O = oracle_lib
+    npdt = np.float64 if dtype == "f64" else np.float32
+    n0, n1, n2 = 26, 22, 18
+    dx = (1.0 / (n0 - 2), 1.0 / (n1 - 2), 1.0 / (n2 - 2))
+    if init == "implode":
+        prim = O.init_implode(n0, n1, n2, dx, dtype=npdt)
+    else:
+        prim = O.random_prim(n0, n1, n2, seed=12).astype(npdt)
+    cons = O.prim_to_cons(prim, 1.4)
+    p_ref, c_ref = prim.copy(), cons.copy()
+    O.simulate(p_ref, c_ref, 1.4, dx, 0.4, 20)
+    pg = _t(cuda, prim)
+    cg = euler.prim_to_cons(pg, 1.4)
+    for _ in range(20):
+        dt = euler.time_step(pg, 1.4, dx).item()
+        euler.godunov(pg, cg, 1.4, dx, float(npdt(0.4) * npdt(dt)), exact=True)
+        euler.cons_to_prim(cg, 1.4, out=pg)
+    assert np.array_equal(cg.cpu().numpy(), c_ref)
+    assert np.array_equal(pg.cpu().numpy(), p_ref)
+
+
 def test_godunov_device_dt_matches_host_dt(cuda, euler, oracle_lib):
     O = oracle_lib
     prim = O.random_prim(40, 33, 20, seed=4)
