@@ -2,7 +2,7 @@
 // (simulations/euler_simulation.cpp:20-88) on one GB300.
 //
 //   euler_simulation [--nx 128] [--nt 200] [--output-freq 10] [--cfl 0.49]
-//                    [--gamma 1.4] [--mode fused|operators]
+//                    [--gamma 1.4] [--mode fused|operators|exact]
 //                    [--precision f64|f32c|f32c_hilo|f32] [--out DIR]
 //
 // Defaults are the reference driver's hard-coded values (:25-29).  Every
@@ -16,6 +16,9 @@
 // the state copied to the host only for output.  --mode operators runs the
 // reference's own loop -- time_step, godunov(cfl*dt), cons_to_prim -- through
 // the drop-in operator headers (FP64 or FP32 per --precision f64|f32).
+// --mode exact runs the same loop with godunov replaced by the bit-identical
+// eulr_godunov_exact_{f64,f32}, so that every written pressure field equals
+// the reference loop's bit for bit.
 #include <euler_gb300.h>
 
 #include <cons_to_prim.hpp>
@@ -37,6 +40,7 @@
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -56,7 +60,7 @@ struct Options {
 {
     std::cerr << "usage: " << argv0
               << " [--nx N] [--nt STEPS] [--output-freq K] [--cfl C] [--gamma G]"
-                 " [--mode fused|operators] [--precision f64|f32c|f32c_hilo|f32] [--out DIR]\n";
+                 " [--mode fused|operators|exact] [--precision f64|f32c|f32c_hilo|f32] [--out DIR]\n";
     std::exit(2);
 }
 
@@ -91,7 +95,7 @@ Options parse(int argc, char** argv)
             usage(argv[0]);
         }
     }
-    if (o.nx < 1 || o.nt < 0 || (o.mode != "fused" && o.mode != "operators")) {
+    if (o.nx < 1 || o.nt < 0 || (o.mode != "fused" && o.mode != "operators" && o.mode != "exact")) {
         usage(argv[0]);
     }
     return o;
@@ -167,9 +171,34 @@ double run_fused(Options const& o)
     return std::chrono::duration<double>(end - start).count();
 }
 
-// The reference's loop through the drop-in operator headers.
+// godunov through eulr_godunov_exact_{f64,f32}: the drop-in's arguments,
+// the reference's results bit for bit.
+template <class P, class C, class real_t>
+void godunov_bit_exact(Kokkos::DefaultExecutionSpace const& exec_space, P const& prim_arrays, C const& cons_arrays,
+                       PerfectGas<real_t> const& eos, UniformMesh3d<real_t> const& mesh, real_t const dt)
+{
+    namespace b = euler_gb300_bridge;
+    using ty = b::types<real_t>;
+    auto const& s = prim_arrays.d;
+    int st;
+    if constexpr (std::is_same_v<real_t, double>) {
+        st = eulr_godunov_exact_f64(b::prim_ptrs<typename ty::cprim>(prim_arrays),
+                                    b::cons_ptrs<typename ty::cons>(cons_arrays), b::extent_int(s, 0),
+                                    b::extent_int(s, 1), b::extent_int(s, 2), eos.gamma(), mesh.dx0(), mesh.dx1(),
+                                    mesh.dx2(), dt, b::stream_of(exec_space));
+    } else {
+        st = eulr_godunov_exact_f32(b::prim_ptrs<typename ty::cprim>(prim_arrays),
+                                    b::cons_ptrs<typename ty::cons>(cons_arrays), b::extent_int(s, 0),
+                                    b::extent_int(s, 1), b::extent_int(s, 2), eos.gamma(), mesh.dx0(), mesh.dx1(),
+                                    mesh.dx2(), dt, b::stream_of(exec_space));
+    }
+    b::check(st, "godunov (bit-exact)");
+}
+
+// The reference's loop through the drop-in operator headers; with `exact`,
+// godunov is the bit-identical one.
 template <class real_t>
-double run_operators(Options const& o)
+double run_operators(Options const& o, bool const exact)
 {
     using index_t = int;
     using span = Kokkos::mdspan<real_t, Kokkos::dextents<index_t, 3>, Kokkos::layout_left>;
@@ -189,8 +218,13 @@ double run_operators(Options const& o)
     auto const start = std::chrono::steady_clock::now();
     for (int it = 1; it <= o.nt; ++it) {
         real_t const dt = time_step(exec_space, as_const(prim_arrays), eos, mesh);
-        godunov(exec_space, as_const(prim_arrays), cons_arrays, eos, mesh, riemann_solver,
-                static_cast<real_t>(o.cfl) * dt);
+        if (exact) {
+            godunov_bit_exact(exec_space, as_const(prim_arrays), cons_arrays, eos, mesh,
+                              static_cast<real_t>(o.cfl) * dt);
+        } else {
+            godunov(exec_space, as_const(prim_arrays), cons_arrays, eos, mesh, riemann_solver,
+                    static_cast<real_t>(o.cfl) * dt);
+        }
         cons_to_prim(exec_space, as_const(cons_arrays), prim_arrays, eos);
         if (o.output_freq > 0 && it % o.output_freq == 0) {
             std::string const name = output_name(o, it);
@@ -217,9 +251,9 @@ int main(int argc, char** argv)
     if (o.mode == "fused") {
         seconds = run_fused(o);
     } else if (o.precision == "f32") {
-        seconds = run_operators<float>(o);
+        seconds = run_operators<float>(o, o.mode == "exact");
     } else {
-        seconds = run_operators<double>(o);
+        seconds = run_operators<double>(o, o.mode == "exact");
     }
     double const cells_updated = o.nt * static_cast<double>(o.nx) * o.nx * o.nx;
     std::cout << cells_updated / seconds * 1e-6 << '\n';
