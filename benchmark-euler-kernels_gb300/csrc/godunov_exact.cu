@@ -8,11 +8,24 @@
 // hllc.hpp:50-105 operation by operation, every product, quotient, sum and
 // square root rounded separately (__dmul_rn, __ddiv_rn, ...; no FMA) in the
 // reference's evaluation order, with the reference's divisions and its
-// two-sided pstar.  One thread per interior cell solves the cell's six
-// faces as the reference loop does (each interior face is solved by both of
-// its cells; both get the same bits, since they call the same function on
-// the same arguments).  It is FP64-bound and about four times slower than
-// the default path.
+// two-sided pstar.
+//
+// The reference solves each interior face twice, once from each of its
+// cells, and recomputes a cell's sound speed and total energy for every
+// face it touches.  Both are the same function on the same arguments, so
+// their bits do not depend on which cell asks: here each face is solved
+// once and each cell's sound speed and total energy computed once, and the
+// results are still the reference's.  A CTA owns a 16 x 8 column of cells
+// and marches through a chunk of z-planes:
+//   * two plane buffers in shared memory hold d, p, u0..u2, the sound speed
+//     and the total energy of an 18 x 10 plane (the tile and its x/y halo);
+//   * per plane, the 136 x-faces and 144 y-faces (one index space, 280
+//     faces for 128 threads) are solved into shared memory, and each thread
+//     solves the z-face above its cell into registers (the one below is the
+//     previous plane's);
+//   * each cell then sums ds_a (F_R - F_L) over a = 0, 1, 2 from zero and
+//     subtracts dtodv times the sum from cons, as godunov.hpp:82-90 does.
+// It is FP64-bound.
 #include "euler_device.cuh"
 #include "kernels.h"
 
@@ -20,10 +33,19 @@ namespace eulr {
 
 namespace {
 
-template <class T>
-struct ExactPrim {
-    T d, p, u[3];
-};
+constexpr int kExTX = 16;                                     // tile cells along i
+constexpr int kExTY = 8;                                      // tile cells along j
+constexpr int kExNT = kExTX * kExTY;                          // threads per CTA
+constexpr int kExPW = kExTX + 2;                              // plane buffer row (tile + x halo)
+constexpr int kExPC = kExPW * (kExTY + 2);                    // plane buffer cells
+constexpr int kExNX = (kExTX + 1) * kExTY;                    // x-faces of a tile plane
+constexpr int kExNF = kExNX + kExTX * (kExTY + 1);            // x- and y-faces of a tile plane
+static_assert(kExNF <= 3 * kExNT && kExPC <= 2 * kExNT, "the face and load loops take at most three and two passes");
+
+// Fields of a plane buffer: the prim fields in the global order, then the
+// sound speed and the total energy of each cell.
+constexpr int kFieldC = 5;
+constexpr int kFieldE = 6;
 
 // Kokkos::min / Kokkos::max on two values (the reference's helpers): the
 // first argument unless the second is strictly smaller / larger.
@@ -38,100 +60,148 @@ __device__ __forceinline__ T kmax(T a, T b)
     return (a < b) ? b : a;
 }
 
-// PerfectGas::speed_of_sound: sqrt(gamma * p / rho) (perfect_gas.hpp:15-18).
+// hllc::operator() (hllc.hpp:50-105) across the face between cell ca of
+// plane A (left) and cell cb of plane B (right), normal direction dir.
+// The flux comes back as (d, e, normal momentum, tangential momenta along
+// t1 < t2).  PerfectGas::speed_of_sound (perfect_gas.hpp:15-18) and the
+// total energy (euler_arrays.hpp:38-42) come from the plane buffers, where
+// each was computed once per cell with the reference's operations.
 template <class T>
-__device__ __forceinline__ T sound_speed_exact(T gamma, T d, T p)
+__device__ __forceinline__ void solve_face_exact(T const (*A)[kExPC], int ca, T const (*B)[kExPC], int cb, int dir,
+                                                 T f[5])
 {
-    return sqrt_rn(div_rn(mul_rn(gamma, p), d));
-}
-
-// hllc::operator() for normal direction dir (hllc.hpp:50-105); the flux in
-// the global field order (d, e, mx0, mx1, mx2).
-template <class T>
-__device__ __forceinline__ void hllc_exact(int dir, T gamma, T gm1, ExactPrim<T> const& L, ExactPrim<T> const& R,
-                                           T f[5])
-{
-    T const un_L = L.u[dir];
-    T const un_R = R.u[dir];
-    T const c_L = sound_speed_exact(gamma, L.d, L.p);
-    T const c_R = sound_speed_exact(gamma, R.d, R.p);
+    int const t1 = dir == 0 ? 1 : 0;
+    int const t2 = dir == 2 ? 1 : 2;
+    T const d_L = A[0][ca], p_L = A[1][ca], un_L = A[2 + dir][ca], c_L = A[kFieldC][ca];
+    T const d_R = B[0][cb], p_R = B[1][cb], un_R = B[2 + dir][cb], c_R = B[kFieldC][cb];
     T const S_L = sub_rn(kmin(un_L, un_R), kmax(c_L, c_R));
     T const S_R = add_rn(kmax(un_L, un_R), kmax(c_L, c_R));
-    T const rc_L = mul_rn(L.d, sub_rn(S_L, un_L));
-    T const rc_R = mul_rn(R.d, sub_rn(S_R, un_R));
+    T const rc_L = mul_rn(d_L, sub_rn(S_L, un_L));
+    T const rc_R = mul_rn(d_R, sub_rn(S_R, un_R));
     // acoustic star state: q_R.p - q_L.p + rc_L * un_L - rc_R * un_R, left to right
-    T const ustar = div_rn(sub_rn(add_rn(sub_rn(R.p, L.p), mul_rn(rc_L, un_L)), mul_rn(rc_R, un_R)), sub_rn(rc_L, rc_R));
-    T const pstar = mul_rn(T(0.5), add_rn(add_rn(add_rn(L.p, R.p), mul_rn(rc_L, sub_rn(ustar, un_L))),
+    T const ustar = div_rn(sub_rn(add_rn(sub_rn(p_R, p_L), mul_rn(rc_L, un_L)), mul_rn(rc_R, un_R)), sub_rn(rc_L, rc_R));
+    T const pstar = mul_rn(T(0.5), add_rn(add_rn(add_rn(p_L, p_R), mul_rn(rc_L, sub_rn(ustar, un_L))),
                                           mul_rn(rc_R, sub_rn(ustar, un_R))));
     bool const left = ustar > T(0);
+    T const (*Q)[kExPC] = left ? A : B;
+    int const cq = left ? ca : cb;
     T const S = left ? S_L : S_R;
-    ExactPrim<T> const& q = left ? L : R;
-    T const un = q.u[dir];
-    // eos.internal_energy(q.d, q.p) + kinetic_energy(q) (euler_arrays.hpp:38-42)
-    T const ke = div_rn(mul_rn(q.d, add_rn(add_rn(mul_rn(q.u[0], q.u[0]), mul_rn(q.u[1], q.u[1])),
-                                           mul_rn(q.u[2], q.u[2]))),
-                        T(2));
-    T const etot = add_rn(div_rn(q.p, gm1), ke);
+    T const d = left ? d_L : d_R;
+    T const p = left ? p_L : p_R;
+    T const un = left ? un_L : un_R;
+    T const etot = Q[kFieldE][cq];
     bool const supersonic = mul_rn(S_L, S_R) > T(0);
     T const un_o = supersonic ? un : ustar;
-    T const ptot_o = supersonic ? q.p : pstar;
+    T const ptot_o = supersonic ? p : pstar;
     T const ratio = div_rn(sub_rn(S, un), sub_rn(S, un_o));
-    T const d_o = mul_rn(ratio, q.d);
-    T const etot_o = add_rn(mul_rn(ratio, etot), div_rn(sub_rn(mul_rn(ptot_o, un_o), mul_rn(q.p, un)), sub_rn(S, ustar)));
+    T const d_o = mul_rn(ratio, d);
+    T const etot_o = add_rn(mul_rn(ratio, etot), div_rn(sub_rn(mul_rn(ptot_o, un_o), mul_rn(p, un)), sub_rn(S, ustar)));
     T const m = mul_rn(d_o, un_o);
     f[0] = m;
     f[1] = mul_rn(add_rn(etot_o, ptot_o), un_o);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        f[2 + a] = a == dir ? add_rn(mul_rn(m, un_o), ptot_o) : mul_rn(m, q.u[a]);
+    f[2] = add_rn(mul_rn(m, un_o), ptot_o);
+    f[3] = mul_rn(m, Q[2 + t1][cq]);
+    f[4] = mul_rn(m, Q[2 + t2][cq]);
+}
+
+// Loads plane k of the tile and its x/y halo (cells outside the array are
+// skipped; no face reads them) with each cell's sound speed
+// sqrt(gamma p / d) and total energy p / (gamma - 1) + d |u|^2 / 2.
+template <class T>
+__device__ __forceinline__ void load_plane_exact(T (*P)[kExPC], CBundle<T> const& prim, Geom const& g, int i0, int j0,
+                                                 int k, T gamma, T gm1)
+{
+    for (int t = threadIdx.x; t < kExPC; t += kExNT) {
+        int const i = i0 - 1 + t % kExPW;
+        int const j = j0 - 1 + t / kExPW;
+        if (i < g.n0 && j < g.n1) {
+            long long const c = g.at(i, j, k);
+            T const d = prim.f[0][c], p = prim.f[1][c];
+            T const u0 = prim.f[2][c], u1 = prim.f[3][c], u2 = prim.f[4][c];
+            P[0][t] = d;
+            P[1][t] = p;
+            P[2][t] = u0;
+            P[3][t] = u1;
+            P[4][t] = u2;
+            P[kFieldC][t] = sqrt_rn(div_rn(mul_rn(gamma, p), d));
+            T const ke = div_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(2));
+            P[kFieldE][t] = add_rn(div_rn(p, gm1), ke);
+        }
     }
 }
 
+// godunov.hpp:32-91 for the interior cells of one 16 x 8 tile over the
+// interior planes [kb, ke); blockIdx.x = tile, blockIdx.y = plane chunk.
 template <class T>
-__device__ __forceinline__ ExactPrim<T> load_exact(CBundle<T> const& prim, long long c)
+__global__ void __launch_bounds__(kExNT) godunov_exact_kernel(CBundle<T> prim, Bundle<T> cons, Geom g, T gamma, T gm1,
+                                                              T ds0, T ds1, T ds2, T dtodv, int ntx, int kchunk)
 {
-    ExactPrim<T> q;
-    q.d = prim.f[0][c];
-    q.p = prim.f[1][c];
-    q.u[0] = prim.f[2][c];
-    q.u[1] = prim.f[3][c];
-    q.u[2] = prim.f[4][c];
-    return q;
-}
+    __shared__ T planes[2][7][kExPC];
+    __shared__ T faces[5][kExNF];
+    int const i0 = 1 + (blockIdx.x % ntx) * kExTX;
+    int const j0 = 1 + (blockIdx.x / ntx) * kExTY;
+    int const kb = 1 + blockIdx.y * kchunk;
+    int const ke = min(kb + kchunk, g.n2 - 1);
+    int const tx = threadIdx.x % kExTX;
+    int const ty = threadIdx.x / kExTX;
+    bool const mine = i0 + tx <= g.n0 - 2 && j0 + ty <= g.n1 - 2; // this thread's column is interior
+    int const ccell = (tx + 1) + kExPW * (ty + 1);                 // its cell in a plane buffer
 
-// godunov.hpp:32-91 for the interior cells [1, n-1)^3: per axis the fluxes
-// of the cell's two faces, flux += ds[a] * (F_R - F_L) starting from zero,
-// then cons -= dtodv * flux.
-template <class T>
-__global__ void __launch_bounds__(256) godunov_exact_kernel(CBundle<T> prim, Bundle<T> cons, Geom g, T gamma, T gm1,
-                                                            T ds0, T ds1, T ds2, T dtodv)
-{
-    int const ix = g.n0 - 2, iy = g.n1 - 2;
-    long long const n = static_cast<long long>(ix) * iy * (g.n2 - 2);
-    T const ds[3] = {ds0, ds1, ds2};
-    long long const stride[3] = {1, g.s1, g.s2};
-    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < n;
-         t += static_cast<long long>(gridDim.x) * blockDim.x) {
-        int const i = 1 + static_cast<int>(t % ix);
-        long long const r = t / ix;
-        int const j = 1 + static_cast<int>(r % iy);
-        int const k = 1 + static_cast<int>(r / iy);
-        long long const c = g.at(i, j, k);
-        ExactPrim<T> const qc = load_exact(prim, c);
-        T flux[5] = {T(0), T(0), T(0), T(0), T(0)};
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            T fL[5], fR[5];
-            hllc_exact(a, gamma, gm1, load_exact(prim, c - stride[a]), qc, fL);
-            hllc_exact(a, gamma, gm1, qc, load_exact(prim, c + stride[a]), fR);
+    T zlo[5], zhi[5];
+    load_plane_exact(planes[(kb - 1) & 1], prim, g, i0, j0, kb - 1, gamma, gm1);
+    load_plane_exact(planes[kb & 1], prim, g, i0, j0, kb, gamma, gm1);
+    __syncthreads();
+    if (mine) {
+        solve_face_exact(planes[(kb - 1) & 1], ccell, planes[kb & 1], ccell, 2, zlo);
+    }
+    __syncthreads(); // plane kb - 1 is overwritten next
+    for (int k = kb; k < ke; ++k) {
+        T const (*cur)[kExPC] = planes[k & 1];
+        load_plane_exact(planes[(k + 1) & 1], prim, g, i0, j0, k + 1, gamma, gm1);
+        __syncthreads();
+        // x-faces (i-1 | i) for i in [i0, i0 + 16], then y-faces (j-1 | j) for j in [j0, j0 + 8]
+        for (int t = threadIdx.x; t < kExNF; t += kExNT) {
+            bool const xf = t < kExNX;
+            int const u = xf ? t : t - kExNX;
+            int const a = xf ? u % (kExTX + 1) : u % kExTX;
+            int const b = xf ? u / (kExTX + 1) : u / kExTX;
+            bool const need = xf ? (i0 + a <= g.n0 - 1 && j0 + b <= g.n1 - 2)
+                                 : (i0 + a <= g.n0 - 2 && j0 + b <= g.n1 - 1);
+            if (need) {
+                int const cl = xf ? a + kExPW * (b + 1) : (a + 1) + kExPW * b;
+                int const cr = cl + (xf ? 1 : kExPW);
+                int const dir = xf ? 0 : 1;
+                T f[5];
+                solve_face_exact(cur, cl, cur, cr, dir, f);
+                faces[0][t] = f[0];
+                faces[1][t] = f[1];
+                faces[2 + dir][t] = f[2];
+                faces[xf ? 3 : 2][t] = f[3];
+                faces[4][t] = f[4];
+            }
+        }
+        if (mine) {
+            solve_face_exact(cur, ccell, planes[(k + 1) & 1], ccell, 2, zhi);
+        }
+        __syncthreads();
+        if (mine) {
+            int const xl = tx + (kExTX + 1) * ty;
+            int const yl = kExNX + tx + kExTX * ty;
+            long long const c = g.at(i0 + tx, j0 + ty, k);
+            T const zl[5] = {zlo[0], zlo[1], zlo[3], zlo[4], zlo[2]}; // (d, e, m0, m1, m2)
+            T const zh[5] = {zhi[0], zhi[1], zhi[3], zhi[4], zhi[2]};
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
-                flux[f] = add_rn(flux[f], mul_rn(ds[a], sub_rn(fR[f], fL[f])));
+                T flux = T(0);
+                flux = add_rn(flux, mul_rn(ds0, sub_rn(faces[f][xl + 1], faces[f][xl])));
+                flux = add_rn(flux, mul_rn(ds1, sub_rn(faces[f][yl + kExTX], faces[f][yl])));
+                flux = add_rn(flux, mul_rn(ds2, sub_rn(zh[f], zl[f])));
+                cons.f[f][c] = sub_rn(cons.f[f][c], mul_rn(dtodv, flux));
             }
         }
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
-            cons.f[f][c] = sub_rn(cons.f[f][c], mul_rn(dtodv, flux[f]));
+            zlo[f] = zhi[f];
         }
     }
 }
@@ -142,7 +212,6 @@ template <class T>
 cudaError_t launch_godunov_exact(CBundle<T> prim, Bundle<T> cons, Geom g, T gamma, T dx0, T dx1, T dx2, T dt,
                                  int sms, cudaStream_t s)
 {
-    long long const n = static_cast<long long>(g.n0 - 2) * (g.n1 - 2) * (g.n2 - 2);
     if (g.n0 < 3 || g.n1 < 3 || g.n2 < 3) {
         return cudaSuccess; // no interior cell
     }
@@ -153,13 +222,23 @@ cudaError_t launch_godunov_exact(CBundle<T> prim, Bundle<T> cons, Geom g, T gamm
     T const ds2 = dx0 * dx1;
     T const dv = (dx0 * dx1) * dx2;
     T const dtodv = dt / dv;
-    long long blocks = (n + 255) / 256;
-    long long const cap = static_cast<long long>(sms) * 8;
-    if (blocks > cap) {
-        blocks = cap;
+    long long const ntx = (g.n0 - 2 + kExTX - 1) / kExTX;
+    long long const tiles = ntx * ((g.n1 - 2 + kExTY - 1) / kExTY);
+    int const planes = g.n2 - 2;
+    if (tiles > 0x7fffffffLL) {
+        return cudaErrorInvalidConfiguration;
     }
-    godunov_exact_kernel<T><<<static_cast<int>(blocks), 256, 0, s>>>(prim, cons, g, gamma, gamma - T(1), ds0, ds1, ds2,
-                                                                    dtodv);
+    // Split the planes into chunks of at least 8 until there are about 64
+    // CTAs per SM to spread, so that the last wave is a small part.
+    long long want = (64LL * sms + tiles - 1) / tiles;
+    long long const most = planes / 8 > 1 ? planes / 8 : 1;
+    want = want < 1 ? 1 : (want > most ? most : want);
+    want = want > 65535 ? 65535 : want;
+    int const kchunk = static_cast<int>((planes + want - 1) / want);
+    int const nchunks = (planes + kchunk - 1) / kchunk;
+    dim3 const grid(static_cast<unsigned>(tiles), static_cast<unsigned>(nchunks));
+    godunov_exact_kernel<T><<<grid, kExNT, 0, s>>>(prim, cons, g, gamma, gamma - T(1), ds0, ds1, ds2, dtodv,
+                                                   static_cast<int>(ntx), kchunk);
     return cudaGetLastError();
 }
 

@@ -191,9 +191,10 @@ int eulr_godunov_f32(eulr_prim_cf32 prim, eulr_cons_f32 cons, int n0, int n1, in
 /* godunov bit-identical to the reference (euler_operators/godunov.hpp:15-92,
  * hllc.hpp:50-105 compiled without FMA contraction): the same arguments and
  * result as eulr_godunov_*, computed in the reference's operation order with
- * every operation rounded separately and each face solved by both of its
- * cells.  For validation against the reference; about four times slower
- * than eulr_godunov_*. */
+ * every operation rounded separately.  Each face is solved once and shared by
+ * its two cells, which gives the bits the reference gets by solving it from
+ * both.  For validation against the reference; about twice as slow as
+ * eulr_godunov_*. */
 int eulr_godunov_exact_f64(eulr_prim_cf64 prim, eulr_cons_f64 cons, int n0, int n1, int n2, double gamma, double dx0,
                            double dx1, double dx2, double dt, eulr_stream_t stream);
 int eulr_godunov_exact_f32(eulr_prim_cf32 prim, eulr_cons_f32 cons, int n0, int n1, int n2, float gamma, float dx0,

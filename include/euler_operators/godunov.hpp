@@ -6,7 +6,7 @@
 // each interior face from both sides); results agree with the reference
 // within 1e-12 relative L-infinity in FP64.  Defining EULR_GODUNOV_BIT_EXACT
 // before including this header routes it to eulr_godunov_exact_{f64,f32}
-// instead: the reference's results bit for bit, about four times slower.
+// instead: the reference's results bit for bit, about twice as slow.
 // Enqueued on the execution space's stream; returns without waiting.
 #pragma once
 

@@ -97,11 +97,14 @@ def test_exact_godunov_matches_reference_fixtures(cuda, euler, path):
 
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
 @pytest.mark.parametrize("shape,dx", [((70, 40, 37), (0.02, 0.03, 0.05)), ((33, 34, 35), (0.1, 0.1, 0.1)),
-                                      ((3, 3, 3), (1.0, 1.0, 1.0)), ((2, 9, 9), (0.5, 0.25, 0.125))])
+                                      ((3, 3, 3), (1.0, 1.0, 1.0)), ((2, 9, 9), (0.5, 0.25, 0.125)),
+                                      ((19, 3, 130), (0.05, 0.5, 0.01)), ((3, 27, 12), (0.3, 0.02, 0.1))])
 def test_exact_godunov_bit_identical_to_oracle(cuda, euler, oracle_lib, dtype, shape, dx):
     """The exact godunov equals the oracle's, itself bit-identical to the
     reference build, on seeded random states (including supersonic faces),
-    ragged, tiny and degenerate grids."""
+    ragged, tiny and degenerate grids: partial 16 x 8 tiles in i and j, one
+    row or one column of cells, and interiors split into several plane
+    chunks."""
     O = oracle_lib
     prim = O.random_prim(*shape, seed=sum(shape))
     if dtype == "f32":
