@@ -124,7 +124,9 @@ __device__ __forceinline__ void load_plane_exact(T (*P)[kExPC], CBundle<T> const
             P[3][t] = u1;
             P[4][t] = u2;
             P[kFieldC][t] = sqrt_rn(div_rn(mul_rn(gamma, p), d));
-            T const ke = div_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(2));
+            // the reference's "/ 2" as "* 0.5": both are the correctly rounded
+            // value of the same real number, so the bits are equal
+            T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
             P[kFieldE][t] = add_rn(div_rn(p, gm1), ke);
         }
     }
