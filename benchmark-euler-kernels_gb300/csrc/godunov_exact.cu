@@ -106,10 +106,12 @@ __device__ __forceinline__ void solve_face_exact(T const (*A)[kExPC], int ca, T 
 
 // Loads plane k of the tile and its x/y halo (cells outside the array are
 // skipped; no face reads them) with each cell's sound speed
-// sqrt(gamma p / d) and total energy p / (gamma - 1) + d |u|^2 / 2.
+// sqrt(gamma p / d) and total energy p / (gamma - 1) + d |u|^2 / 2.  The
+// quotient by the constant gamma - 1 is the correctly rounded one formed
+// from rgm1 = RN(1 / (gamma - 1)) (div_by_rcp), as prim_to_cons forms it.
 template <class T>
 __device__ __forceinline__ void load_plane_exact(T (*P)[kExPC], CBundle<T> const& prim, Geom const& g, int i0, int j0,
-                                                 int k, T gamma, T gm1)
+                                                 int k, T gamma, T gm1, T rgm1)
 {
     for (int t = threadIdx.x; t < kExPC; t += kExNT) {
         int const i = i0 - 1 + t % kExPW;
@@ -127,7 +129,7 @@ __device__ __forceinline__ void load_plane_exact(T (*P)[kExPC], CBundle<T> const
             // the reference's "/ 2" as "* 0.5": both are the correctly rounded
             // value of the same real number, so the bits are equal
             T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
-            P[kFieldE][t] = add_rn(div_rn(p, gm1), ke);
+            P[kFieldE][t] = add_rn(div_by_rcp(p, gm1, rgm1), ke);
         }
     }
 }
@@ -136,7 +138,8 @@ __device__ __forceinline__ void load_plane_exact(T (*P)[kExPC], CBundle<T> const
 // interior planes [kb, ke); blockIdx.x = tile, blockIdx.y = plane chunk.
 template <class T>
 __global__ void __launch_bounds__(kExNT) godunov_exact_kernel(CBundle<T> prim, Bundle<T> cons, Geom g, T gamma, T gm1,
-                                                              T ds0, T ds1, T ds2, T dtodv, int ntx, int kchunk)
+                                                              T rgm1, T ds0, T ds1, T ds2, T dtodv, int ntx,
+                                                              int kchunk)
 {
     __shared__ T planes[2][7][kExPC];
     __shared__ T faces[5][kExNF];
@@ -150,8 +153,8 @@ __global__ void __launch_bounds__(kExNT) godunov_exact_kernel(CBundle<T> prim, B
     int const ccell = (tx + 1) + kExPW * (ty + 1);                 // its cell in a plane buffer
 
     T zlo[5], zhi[5];
-    load_plane_exact(planes[(kb - 1) & 1], prim, g, i0, j0, kb - 1, gamma, gm1);
-    load_plane_exact(planes[kb & 1], prim, g, i0, j0, kb, gamma, gm1);
+    load_plane_exact(planes[(kb - 1) & 1], prim, g, i0, j0, kb - 1, gamma, gm1, rgm1);
+    load_plane_exact(planes[kb & 1], prim, g, i0, j0, kb, gamma, gm1, rgm1);
     __syncthreads();
     if (mine) {
         solve_face_exact(planes[(kb - 1) & 1], ccell, planes[kb & 1], ccell, 2, zlo);
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(kExNT) godunov_exact_kernel(CBundle<T> prim, B
     __syncthreads(); // plane kb - 1 is overwritten next
     for (int k = kb; k < ke; ++k) {
         T const (*cur)[kExPC] = planes[k & 1];
-        load_plane_exact(planes[(k + 1) & 1], prim, g, i0, j0, k + 1, gamma, gm1);
+        load_plane_exact(planes[(k + 1) & 1], prim, g, i0, j0, k + 1, gamma, gm1, rgm1);
         __syncthreads();
         // x-faces (i-1 | i) for i in [i0, i0 + 16], then y-faces (j-1 | j) for j in [j0, j0 + 8]
         for (int t = threadIdx.x; t < kExNF; t += kExNT) {
@@ -239,7 +242,8 @@ cudaError_t launch_godunov_exact(CBundle<T> prim, Bundle<T> cons, Geom g, T gamm
     int const kchunk = static_cast<int>((planes + want - 1) / want);
     int const nchunks = (planes + kchunk - 1) / kchunk;
     dim3 const grid(static_cast<unsigned>(tiles), static_cast<unsigned>(nchunks));
-    godunov_exact_kernel<T><<<grid, kExNT, 0, s>>>(prim, cons, g, gamma, gamma - T(1), ds0, ds1, ds2, dtodv,
+    T const gm1 = gamma - T(1);
+    godunov_exact_kernel<T><<<grid, kExNT, 0, s>>>(prim, cons, g, gamma, gm1, T(1) / gm1, ds0, ds1, ds2, dtodv,
                                                    static_cast<int>(ntx), kchunk);
     return cudaGetLastError();
 }
