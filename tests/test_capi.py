@@ -88,3 +88,15 @@ def test_invalid_arguments_rejected_without_gpu(euler):
 def test_missing_library_fails_loudly(euler, tmp_path):
     with pytest.raises(FileNotFoundError):
         euler.load(str(tmp_path / "libeuler_gb300.so"))
+
+
+@pytest.mark.parametrize("args", [["--mode", "bogus"], ["--nx", "0"], ["--nt", "-1"], ["--unknown"]])
+def test_driver_rejects_bad_arguments_without_gpu(euler, args):
+    """The implosion driver validates its options before any CUDA call: a bad
+    mode, size or flag prints the usage line (which names every mode) and
+    exits 2."""
+    from euler_gb300.build import app_path
+
+    r = subprocess.run([app_path("euler_simulation"), *args], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2, (args, r.stdout, r.stderr)
+    assert "--mode fused|operators|exact" in r.stdout + r.stderr
