@@ -234,6 +234,7 @@ struct TileCtx {
     unsigned inflight;        // bit s: a TMA into slot s has not been waited for
     bool timed_out;           // a bounded mbarrier wait ran out
     long long wkey;           // ordered bits of this thread's max wavespeed (FP64)
+    unsigned wrun;            // FP64 step: the warp's running max of wavespeed estimates (WaveScreen)
     float wmaxf;              // this thread's max wavespeed (FP32 states: keyed once, at the flush)
     bool bad;                 // this thread saw a non-physical cell
 };
@@ -312,6 +313,12 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
             c.inflight |= 1u;
         }
     }
+
+    // FP64 step: the next step's CFL wavespeed is screened (WaveScreen); the
+    // running max carries over from the CTA's previous item of the same grid
+    constexpr bool kScreen = sizeof(T) == 8 && MODE == kModeStep;
+    WaveScreen screen(p.gamma, p.invdx0, p.invdx1, p.invdx2);
+    screen.run = c.wrun;
 
     for (int k = kb; k < ke; ++k) {
         int const cur = (k - kb + 1) % NSLOT;
@@ -410,6 +417,7 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
         for (int f = 0; f < 5; ++f) {
             fza[f] = fz[f * L::NFZ + tid];
         }
+        T wv[4] = {T(0), T(0), T(0), T(0)}; // FP64 step: the new cs, v0, v1, v2, for the screened wavespeed
         if (own) {
             int const xl = tj * (TX + 1) + ti;
             int const yb = tj * TX + ti;
@@ -472,18 +480,41 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
                     }
                     p.cs_out[o] = cs;
                 }
-                // next step's CFL wavespeed (time_step.hpp:28-33)
-                // (cubic cells: one product instead of three)
-                T const invdt = cubic ? (T(3) * cs + abs_(v0) + abs_(v1) + abs_(v2)) * p.invdx0
-                                      : (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 +
-                                                (cs + abs_(v2)) * p.invdx2;
-                if constexpr (sizeof(T) == 4) {
-                    c.wmaxf = fmaxf(c.wmaxf, invdt); // NaN never wins (fmaxf returns the other operand)
+                if constexpr (kScreen) {
+                    wv[0] = cs;
+                    wv[1] = v0;
+                    wv[2] = v1;
+                    wv[3] = v2;
+                    c.bad |= !(finite_positive(u[0]) && finite_positive(pr)); // the wavespeed is checked below
                 } else {
-                    long long const key = wave_key(invdt);
-                    c.wkey = key > c.wkey ? key : c.wkey;
+                    // next step's CFL wavespeed (time_step.hpp:28-33)
+                    // (cubic cells: one product instead of three)
+                    T const invdt = cubic ? (T(3) * cs + abs_(v0) + abs_(v1) + abs_(v2)) * p.invdx0
+                                          : (cs + abs_(v0)) * p.invdx0 + (cs + abs_(v1)) * p.invdx1 +
+                                                    (cs + abs_(v2)) * p.invdx2;
+                    if constexpr (sizeof(T) == 4) {
+                        c.wmaxf = fmaxf(c.wmaxf, invdt); // NaN never wins (fmaxf returns the other operand)
+                    } else {
+                        long long const key = wave_key(invdt);
+                        c.wkey = key > c.wkey ? key : c.wkey;
+                    }
+                    c.bad |= !cell_ok(u[0], pr, invdt);
                 }
-                c.bad |= !cell_ok(u[0], pr, invdt);
+            }
+        }
+        if constexpr (kScreen) {
+            // next step's CFL wavespeed (time_step.hpp:28-33), in FP64 only
+            // for the cells that can hold the max; the same expression as
+            // the unscreened step, so the max and the dt are unchanged.
+            // Every lane of the warp is here (the screen is warp-collective);
+            // a non-finite wavespeed always takes the FP64 branch.
+            if (screen.step_exact_needed(own, wv[0], wv[1], wv[2], wv[3], cubic)) {
+                T const invdt = cubic ? (T(3) * wv[0] + abs_(wv[1]) + abs_(wv[2]) + abs_(wv[3])) * p.invdx0
+                                      : (wv[0] + abs_(wv[1])) * p.invdx0 + (wv[0] + abs_(wv[2])) * p.invdx1 +
+                                                (wv[0] + abs_(wv[3])) * p.invdx2;
+                long long const key = wave_key(invdt);
+                c.wkey = key > c.wkey ? key : c.wkey;
+                c.bad |= dbits(invdt) >= kInfBits;
             }
         }
         // the z face above becomes the next plane's z face below
@@ -493,6 +524,7 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
         }
         __syncthreads(); // fluxes are rewritten by the next face phase
     }
+    c.wrun = screen.run;
     return !__syncthreads_or(c.timed_out);
 }
 
@@ -538,6 +570,7 @@ __device__ __forceinline__ void flush_wavespeed(TileCtx<T>& c, unsigned long lon
         }
     }
     c.wkey = 0;
+    c.wrun = 0u; // the next item may be another grid's
     c.wmaxf = 0.0f;
     c.bad = false;
 }
@@ -558,6 +591,7 @@ __device__ __forceinline__ TileCtx<T> make_ctx(unsigned char* smem_dyn)
     c.inflight = 0;
     c.timed_out = false;
     c.wkey = 0;
+    c.wrun = 0u;
     c.wmaxf = 0.0f;
     c.bad = false;
     return c;

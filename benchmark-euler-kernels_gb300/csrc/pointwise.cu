@@ -87,68 +87,6 @@ __global__ void __launch_bounds__(256) cons_to_prim_kernel(CBundle<T> cons, Bund
     }
 }
 
-// ------------------------------------------ exact max wavespeed, screened
-// The CFL step needs the max over cells of the reference's wavespeed
-// (time_step.hpp:28-33; cell_invdt_exact: a correctly rounded FP64 division
-// and square root per cell, about 25 FP64 issue slots), exactly.  But the
-// exact value is needed only where it can be the max, so an FP32 estimate
-// screens the cells, with no FP64 instruction at all: its inputs are built
-// from the doubles' high words on the integer pipe (the mantissa truncated to
-// 20 bits, a relative error in (-2^-20, 0]) and the rest runs on the FP32
-// pipe.  Where rho, p and gamma p/rho lie in [1e-30, 1e30] and the estimate
-// is at most 1e30, its relative error is below 2^-20 + 5 * 2^-24 to first
-// order: p/rho carries under 2^-20 (both truncations go toward zero), the
-// square root halves it, |u| carries under 2^-20, and gamma, 1/dx and eight
-// FP32 operations add 2^-24 each along any path.  Two estimates can thus
-// misorder cells by at most 2.7 * 2^-20 relative, 42 FP32 ulps; a cell is
-// evaluated exactly when its estimate is within 128 ulps of the warp's
-// running max of estimates.  Every other cell -- NaN, infinite or
-// out-of-range values -- is always evaluated exactly.  So the cell holding
-// the exact max is always evaluated, and the max of the exact values over
-// the evaluated cells is the exact max.  The evaluated cells are essentially
-// each warp's running-max records: a few per ten thousand on random states.
-struct WaveScreen {
-    float g, ix0, ix1, ix2;
-    bool on;        // gamma and 1/dx in FP32's safe range: screening is sound
-    unsigned run;   // the warp's running max of the estimates' bit patterns
-
-    __device__ __forceinline__ static bool in_range(float x) { return x >= 1e-30f && x <= 1e30f; }
-
-    // x with its mantissa truncated to 20 bits, from the high word alone: 0
-    // below FP32's normal range, infinity above it (and for NaN).
-    __device__ __forceinline__ static float high_word_float(double x)
-    {
-        unsigned const hi = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(x)) >> 32);
-        int const e = static_cast<int>((hi >> 20) & 0x7ffu) - (1023 - 127);
-        unsigned const mag = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : (static_cast<unsigned>(e) << 23) | ((hi & 0xfffffu) << 3));
-        return __uint_as_float((hi & 0x80000000u) | mag);
-    }
-
-    __device__ __forceinline__ WaveScreen(double gamma, double x0, double x1, double x2)
-        : g(static_cast<float>(gamma)), ix0(static_cast<float>(x0)), ix1(static_cast<float>(x1)),
-          ix2(static_cast<float>(x2)), run(0u)
-    {
-        on = in_range(g) && in_range(ix0) && in_range(ix1) && in_range(ix2);
-    }
-
-    // Warp-collective (all 32 lanes call it together): true when this lane's
-    // cell (if valid) needs its exact wavespeed.
-    __device__ __forceinline__ bool exact_needed(bool valid, double d, double p, double u0, double u1, double u2)
-    {
-        float const d32 = high_word_float(d);
-        float const p32 = high_word_float(p);
-        float const x32 = __fdiv_rn(g * p32, d32);
-        float const c32 = __fsqrt_rn(x32);
-        float const v32 = (c32 + fabsf(high_word_float(u0))) * ix0 + (c32 + fabsf(high_word_float(u1))) * ix1 +
-                          (c32 + fabsf(high_word_float(u2))) * ix2;
-        bool const sure = on && in_range(d32) && in_range(p32) && in_range(x32) && v32 <= 1e30f;
-        unsigned const key = (valid && sure) ? __float_as_uint(v32) : 0u;
-        unsigned const m = __reduce_max_sync(0xffffffffu, key);
-        run = m > run ? m : run;
-        return valid && (!sure || key + 128u >= run);
-    }
-};
-
 // --------------------------------------------------------------- time_step
 // time_step.hpp:22-39.  The reference takes min over cells of 1/invdt; since
 // correctly rounded division is monotonic, min_c RN(1/x_c) = RN(1/max_c x_c),

@@ -107,5 +107,91 @@ inline int choose_kchunk(int columns, int iz, long long slots)
     return best;
 }
 
+// ------------------------------------------ exact max wavespeed, screened
+// The CFL step needs the max over cells of the reference's wavespeed
+// (time_step.hpp:28-33; cell_invdt_exact: a correctly rounded FP64 division
+// and square root per cell, about 25 FP64 issue slots), exactly.  But the
+// exact value is needed only where it can be the max, so an FP32 estimate
+// screens the cells, with no FP64 instruction at all: its inputs are built
+// from the doubles' high words on the integer pipe (the mantissa truncated to
+// 20 bits, a relative error in (-2^-20, 0]) and the rest runs on the FP32
+// pipe.  Where rho, p and gamma p/rho lie in [1e-30, 1e30] and the estimate
+// is at most 1e30, its relative error is below 2^-20 + 5 * 2^-24 to first
+// order: p/rho carries under 2^-20 (both truncations go toward zero), the
+// square root halves it, |u| carries under 2^-20, and gamma, 1/dx and eight
+// FP32 operations add 2^-24 each along any path.  Two estimates can thus
+// misorder cells by at most 2.7 * 2^-20 relative, 42 FP32 ulps; a cell is
+// evaluated exactly when its estimate is within 128 ulps of the warp's
+// running max of estimates.  Every other cell -- NaN, infinite or
+// out-of-range values -- is always evaluated exactly.  So the cell holding
+// the exact max is always evaluated, and the max of the exact values over
+// the evaluated cells is the exact max.  The evaluated cells are essentially
+// each warp's running-max records: a few per ten thousand on random states.
+struct WaveScreen {
+    float g, ix0, ix1, ix2;
+    bool on;        // gamma and 1/dx in FP32's safe range: screening is sound
+    unsigned run;   // the warp's running max of the estimates' bit patterns
+
+    __device__ __forceinline__ static bool in_range(float x) { return x >= 1e-30f && x <= 1e30f; }
+
+    // x with its mantissa truncated to 20 bits, from the high word alone: 0
+    // below FP32's normal range, infinity above it (and for NaN).
+    __device__ __forceinline__ static float high_word_float(double x)
+    {
+        unsigned const hi = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(x)) >> 32);
+        int const e = static_cast<int>((hi >> 20) & 0x7ffu) - (1023 - 127);
+        unsigned const mag = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : (static_cast<unsigned>(e) << 23) | ((hi & 0xfffffu) << 3));
+        return __uint_as_float((hi & 0x80000000u) | mag);
+    }
+
+    __device__ __forceinline__ WaveScreen(double gamma, double x0, double x1, double x2)
+        : g(static_cast<float>(gamma)), ix0(static_cast<float>(x0)), ix1(static_cast<float>(x1)),
+          ix2(static_cast<float>(x2)), run(0u)
+    {
+        on = in_range(g) && in_range(ix0) && in_range(ix1) && in_range(ix2);
+    }
+
+    // Warp-collective (all 32 lanes call it together): true when this lane's
+    // cell (if valid) needs its exact wavespeed.
+    __device__ __forceinline__ bool exact_needed(bool valid, double d, double p, double u0, double u1, double u2)
+    {
+        float const d32 = high_word_float(d);
+        float const p32 = high_word_float(p);
+        float const x32 = __fdiv_rn(g * p32, d32);
+        float const c32 = __fsqrt_rn(x32);
+        float const v32 = (c32 + fabsf(high_word_float(u0))) * ix0 + (c32 + fabsf(high_word_float(u1))) * ix1 +
+                          (c32 + fabsf(high_word_float(u2))) * ix2;
+        bool const sure = on && in_range(d32) && in_range(p32) && in_range(x32) && v32 <= 1e30f;
+        unsigned const key = (valid && sure) ? __float_as_uint(v32) : 0u;
+        unsigned const m = __reduce_max_sync(0xffffffffu, key);
+        run = m > run ? m : run;
+        return valid && (!sure || key + 128u >= run);
+    }
+
+    // The fused FP64 step's form (warp-collective as well).  The step has the
+    // new state's faithful sound speed cs and its velocities, and its
+    // wavespeed is (3 cs + |v0| + |v1| + |v2|) / dx on cubic cells, else
+    // sum_d (cs + |v_d|) / dx_d.  The estimate truncates cs and |v_d| (each
+    // under 2^-20) and adds at most six FP32 roundings and 1/dx's own, so
+    // its relative error is below 2^-20 + 6 * 2^-24, and two estimates
+    // misorder by at most 44 ulps: the 128-ulp band holds here too.
+    // Velocities below FP32's normal range read as zero: an error under
+    // 2^-26 relative to cs >= 1e-30, far inside the band.
+    __device__ __forceinline__ bool step_exact_needed(bool valid, double cs, double v0, double v1, double v2, bool cubic)
+    {
+        float const c32 = high_word_float(cs);
+        float const a0 = fabsf(high_word_float(v0));
+        float const a1 = fabsf(high_word_float(v1));
+        float const a2 = fabsf(high_word_float(v2));
+        float const v32 = cubic ? (3.0f * c32 + a0 + a1 + a2) * ix0
+                                : (c32 + a0) * ix0 + (c32 + a1) * ix1 + (c32 + a2) * ix2;
+        bool const sure = on && in_range(c32) && v32 <= 1e30f;
+        unsigned const key = (valid && sure) ? __float_as_uint(v32) : 0u;
+        unsigned const m = __reduce_max_sync(0xffffffffu, key);
+        run = m > run ? m : run;
+        return valid && (!sure || key + 128u >= run);
+    }
+};
+
 } // namespace
 } // namespace eulr

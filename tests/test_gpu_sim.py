@@ -229,3 +229,58 @@ def test_objects_release_their_memory_and_report_oom(cuda, euler):
         s.init_implode()
         s.advance(1)
         assert s.status() == 0
+
+
+def _max_wavespeed_dt(prim, gamma, dx, cfl):
+    """cfl / max over cells of sum_d (c + |u_d|) / dx_d (time_step.hpp:28-39),
+    c = sqrt(gamma p / rho), in numpy FP64."""
+    d, p, u0, u1, u2 = (prim[f].astype(np.float64) for f in range(5))
+    c = np.sqrt(gamma * p / d)
+    inv = (c + np.abs(u0)) / dx[0] + (c + np.abs(u1)) / dx[1] + (c + np.abs(u2)) / dx[2]
+    return cfl / inv.max()
+
+
+def _screen_state(kind, shape, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    prim = np.empty((5,) + tuple(reversed(shape)), dtype=np.float64)
+    if kind == "random":
+        prim[0] = np.exp(rng.uniform(np.log(0.1), np.log(10.0), prim[0].shape))
+        prim[1] = np.exp(rng.uniform(np.log(0.1), np.log(10.0), prim[1].shape))
+        prim[2:] = rng.normal(0.0, 1.0, prim[2:].shape)
+    elif kind == "dense_ties":
+        # every cell's wavespeed within 1e-7 of the others: far below the
+        # FP32 estimate's resolution, so the screen must keep them all
+        prim[0] = 1.0
+        prim[1] = 1.0
+        prim[2] = 0.5 * (1.0 + 1e-7 * rng.uniform(0.0, 1.0, prim[2].shape))
+        prim[3] = 0.0
+        prim[4] = 0.0
+    else:  # wide_range: rho and p over 4 decades, |u| over 4 more (wider contrasts leave the physical states)
+        prim[0] = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), prim[0].shape))
+        prim[1] = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), prim[1].shape))
+        prim[2:] = rng.normal(0.0, 1.0, prim[2:].shape) * np.exp(rng.uniform(np.log(1e-2), np.log(1e2), prim[2:].shape))
+    return prim
+
+
+@pytest.mark.parametrize("kind", ["random", "dense_ties", "wide_range"])
+@pytest.mark.parametrize("shape,dx", [((40, 34, 30), (0.02, 0.02, 0.02)), ((41, 34, 30), (0.02, 0.03, 0.025))],
+                         ids=["even_n0_tma_cubic", "odd_n0_plain_loads_non_cubic"])
+def test_step_dt_is_the_max_wavespeed_of_its_state(cuda, euler, kind, shape, dx):
+    """The fused step reduces the next step's CFL wavespeed in the same pass,
+    evaluating it in FP64 only for the cells an FP32 estimate cannot rule out.
+    After one and three steps the dt it keeps is cfl / max wavespeed of the
+    state it wrote, over every cell (ghosts included), within a few ulps of
+    numpy's (the step's sound speed is faithful, not correctly rounded); a
+    cell wrongly screened out would move it by up to the estimate's 2^-16
+    band."""
+    gamma, cfl = 1.4, 0.4
+    prim0 = _screen_state(kind, shape, seed=sum(shape))
+    with euler.Simulation(*shape, gamma, dx, cfl) as sim:
+        sim.set_prim(prim0)
+        for steps in (1, 2):
+            sim.advance(steps)
+            prim, _ = sim.state_numpy()
+            _, dt, _ = sim.time()
+            ref = _max_wavespeed_dt(prim, gamma, dx, cfl)
+            assert abs(dt - ref) <= 1e-14 * ref, (kind, steps, dt, ref)
+        assert sim.status() == 0
