@@ -1,5 +1,5 @@
-"""The screened exact max wavespeed of time_step and the state load
-(csrc/pointwise.cu: WaveScreen), emulated on the host with IEEE float32
+"""The screened exact max wavespeed of time_step, the state load and the
+fused FP64 step (csrc/step_common.cuh: WaveScreen), emulated on the host with IEEE float32
 arithmetic: the FP32 estimate built from the doubles' high words stays within
 its stated error bound, and the warp scan (running max of the estimates'
 bit patterns, exact evaluation within 128 FP32 ulps of it, out-of-range cells
@@ -101,3 +101,67 @@ def test_screen_evaluates_few_cells_on_random_states():
     sure, _, key = screen(d, p, u, (512.0, 512.0, 512.0))
     assert sure.all()
     assert warp_scan(sure, key).mean() < 0.005
+
+
+STEP_BOUND = 2.0 ** -20 + 6 * 2.0 ** -24  # WaveScreen::step_exact_needed
+
+
+def step_screen(cs, u, ix, cubic):
+    """WaveScreen::step_exact_needed: the estimate from the step's own sound
+    speed and velocities (separately rounded FP32; the device may contract a
+    product and a sum into one FMA, which only removes a rounding)."""
+    f = np.float32
+    c32 = high_word_float(cs)
+    a = [np.abs(high_word_float(u[k])) for k in range(3)]
+    if cubic:
+        v32 = (((f(3.0) * c32 + a[0]) + a[1]) + a[2]) * f(ix[0])
+    else:
+        v32 = ((c32 + a[0]) * f(ix[0]) + (c32 + a[1]) * f(ix[1])) + (c32 + a[2]) * f(ix[2])
+    inr = (c32 >= f(1e-30)) & (c32 <= f(1e30))
+    sure = inr & (v32 <= f(1e30))
+    return sure, v32, np.where(sure, v32.view(np.uint32), np.uint32(0)).astype(np.int64)
+
+
+def step_exact(cs, u, ix, cubic):
+    if cubic:
+        return (3.0 * cs + np.abs(u[0]) + np.abs(u[1]) + np.abs(u[2])) * ix[0]
+    return (cs + np.abs(u[0])) * ix[0] + (cs + np.abs(u[1])) * ix[1] + (cs + np.abs(u[2])) * ix[2]
+
+
+def step_cases(rng, n):
+    for name, d, p, u in cases(rng, n):
+        yield name, np.sqrt(GAMMA * p / d), u  # the step's sound speed, to within an ulp
+    # estimates in the wrong order for this form: most cells have
+    # c = 1 + 2^-20 (exact in 20 mantissa bits) and u = 0.25; a few have c
+    # 2^-45 lower (truncated a whole 2^-20 lower) and u0 2^-30 higher (lost in
+    # truncation) -- the larger exact wavespeed behind an estimate about 12
+    # FP32 ulps lower
+    cm = np.full(n, 1.0 + 2.0 ** -20)
+    um = np.full((3, n), 0.25)
+    planted = rng.choice(n, 8, replace=False)
+    cm[planted] -= 2.0 ** -45
+    um[0, planted] += 2.0 ** -30
+    yield "misordered", cm, um
+
+
+def test_step_screen_error_bound_and_no_missed_max():
+    """The fused step's form of the screen: within its bound, and the warp
+    scan keeps the cell holding the exact max, on the same state families
+    and on one whose estimates are misordered."""
+    rng = np.random.default_rng(99)
+    worst = 0.0
+    with np.errstate(all="ignore"):
+        for trial in range(60):
+            cubic = trial % 2 == 1
+            ix = (64.0, 64.0, 64.0) if cubic else (64.0, 57.0, 71.0)
+            for name, cs, u in step_cases(rng, 32 * 64):
+                v = step_exact(cs, u, ix, cubic)
+                sure, v32, key = step_screen(cs, u, ix, cubic)
+                if sure.any():
+                    rel = np.abs(v32[sure].astype(np.float64) / v[sure] - 1.0)
+                    worst = max(worst, float(rel.max()))
+                evaluated = warp_scan(sure, key)
+                finite = np.isfinite(v)
+                m = v[finite].max()
+                assert (evaluated & (v == m)).any(), (name, trial)
+    assert worst <= STEP_BOUND, worst
