@@ -11,10 +11,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def oracle_pressure(O, nx, steps, cfl):
+def oracle_pressure(O, nx, steps, cfl, dtype=np.float64):
     n = nx + 2
     dx = (1.0 / nx,) * 3
-    prim = O.init_implode(n, n, n, dx)
+    prim = O.init_implode(n, n, n, dx, dtype=dtype)
     cons = O.prim_to_cons(prim, 1.4)
     out = {}
     done = 0
@@ -25,19 +25,19 @@ def oracle_pressure(O, nx, steps, cfl):
     return out
 
 
-@pytest.mark.parametrize("mode", ["fused", "operators", "exact"])
-def test_driver_npy_output(cuda, euler, oracle_lib, tmp_path, mode):
+@pytest.mark.parametrize("mode,precision", [("fused", "f64"), ("operators", "f64"), ("exact", "f64"), ("exact", "f32")])
+def test_driver_npy_output(cuda, euler, oracle_lib, tmp_path, mode, precision):
     from euler_gb300.build import app_path
 
     exe = app_path("euler_simulation")
     nx, nt = 24, 20
     r = subprocess.run([exe, "--nx", str(nx), "--nt", str(nt), "--output-freq", "10", "--mode", mode,
-                        "--out", str(tmp_path)], capture_output=True, text=True, timeout=300)
+                        "--precision", precision, "--out", str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     lines = r.stdout.strip().splitlines()
     assert lines[0].startswith("Saving ") and lines[0].endswith("done")
     assert float(lines[-1]) > 0  # Mcell/s
-    ref = oracle_pressure(oracle_lib, nx, (10, 20), 0.49)
+    ref = oracle_pressure(oracle_lib, nx, (10, 20), 0.49, np.float32 if precision == "f32" else np.float64)
     for s in (10, 20):
         path = tmp_path / f"test_{s:010d}.npy"
         hdr = open(path, "rb").read(128)
@@ -48,8 +48,8 @@ def test_driver_npy_output(cuda, euler, oracle_lib, tmp_path, mode):
         got = p.transpose(2, 1, 0)
         if mode == "exact":
             # the reference loop with the bit-identical godunov: every dump
-            # equals the oracle's loop bit for bit
-            assert np.array_equal(got, ref[s]), (mode, s)
+            # equals the oracle's loop bit for bit (real_t = double or float)
+            assert got.dtype == ref[s].dtype and np.array_equal(got, ref[s]), (mode, precision, s)
             continue
         err = np.abs(got - ref[s]).max() / np.abs(ref[s]).max()
         assert err <= 1e-11, (mode, s, err)
