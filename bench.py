@@ -57,9 +57,8 @@ CFL = 0.4
 FLOPS_PER_CELL_DEFAULT = None
 
 # DRAM bytes (read + write) per interior cell of the fused FP64 kernel, from
-# one ncu capture at 192^3 (profiles/flux_step_f64_192.md: 674 MB + 580 MB over
-# 7.08 M interior cells); the kernel streams each plane once, so traffic
-# scales with cells.
+# one ncu capture at 192^3 (674 MB read + 580 MB written over 7.08 M interior
+# cells); the kernel streams each plane once, so traffic scales with cells.
 FLUX_F64_DRAM_BYTES_PER_CELL = 177.3
 
 
@@ -339,7 +338,7 @@ def run_fp32c_leg(torch, E, args, stream, n0, dx, interior, steps_total, prim_re
                         "kernel_ms": flux_ms,
                         "limiter": "instruction issue, not HBM: ncu shows the SM issuing on 75% of cycles at "
                                    "776 thread-instructions per cell, DRAM at the algorithmic 40 B/cell "
-                                   "(profiles/flux_step_f32c_256.md)"}}
+                                   "(ncu at 256^3)"}}
     if hbm_peak:
         out["roofline"]["frac"] = out["roofline"]["achieved"] / hbm_peak
     return out
@@ -622,7 +621,7 @@ def time_ops(torch, E, prim, n_int, fpc=None, fp64_peak=None, hbm_peak=None):
                 rec["fp64_frac"] = rec["fp64_tflops"] * 1e12 / fp64_peak
             if hbm_peak:
                 rec["hbm_frac"] = rec["gb_s"] / hbm_peak
-    # the roofline that bounds each operator on GB300 (profiles/pointwise_ops_f64_256.md)
+    # the roofline that bounds each operator on GB300 (ncu of each operator at 256^3)
     for name in ("prim_to_cons", "cons_to_prim", "godunov", "godunov_exact"):
         out[name]["bound"] = "fp64"
     out["time_step"]["bound"] = "hbm"
@@ -705,7 +704,7 @@ def run_ours(args):
             "step_ms_sum_of_launches": step_ms_launches,
             "traffic": FLUX_F64_DRAM_BYTES_PER_CELL * interior,
             "traffic_note": "dram bytes read+write per launch: 177.3 B per interior cell from an ncu capture at "
-                            "192^3 (profiles/flux_step_f64_192.md), scaled by cells"}
+                            "192^3, scaled by cells"}
     if fpc:
         fl = fpc["fused_step_fp64"] * interior
         roof["achieved"] = fl / (flux_ms * 1e-3) / 1e12

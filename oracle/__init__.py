@@ -32,7 +32,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libeuler_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libeuler_ref.so")
 REF_TLM_SO = os.path.join(HERE, "_ref", "libeuler_ref_tlm.so")
-REFERENCE_DIR = "/root/reference"
+# The reference checkout: $EULER_REFERENCE_DIR, else a directory named
+# "reference" beside this repository's root.
+REFERENCE_DIR = os.environ.get("EULER_REFERENCE_DIR") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 
 _DT = {"f64": (np.float64, ctypes.c_double), "f32": (np.float32, ctypes.c_float)}
 _libs: dict[str, ctypes.CDLL] = {}

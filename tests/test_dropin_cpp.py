@@ -10,8 +10,8 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle import REFERENCE_DIR as REF
 
-REF = "/root/reference"
 INC = [os.path.join(ROOT, "include"), os.path.join(ROOT, "include", "euler_operators"),
        os.path.join(ROOT, "include", "euler_operators_kokkos"), "/usr/local/cuda/include"]
 
