@@ -180,87 +180,86 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------- CPU
-def cpu_baseline(n: int, seconds: float):
-    """The oracle (C restatement of the reference operators, OpenMP over all
-    host cores) on a slab of the workload: n x n x kz interior cells, with kz
-    sized so the run takes about `seconds`."""
+CPU_SLAB_PLANES = 32
+
+
+def cpu_loop_sample(n: int, seconds: float, warmup: int, steps: int | None = None):
+    """Times the reference loop (time_step, godunov, cons_to_prim) of the
+    oracle -- the C restatement of the reference operators, OpenMP on every
+    host core -- on an n x n x kz-interior slab of the workload's random state.
+
+    Both CPU legs (the cpu_baseline leg and the reference arm) call this one
+    sampler on the same slab: kz = max(CPU_SLAB_PLANES, 2 x threads) planes
+    (at most n), so that every thread has rows to work on (godunov shares the
+    (k, j) rows among the threads).  With steps=None the number of timed steps
+    is chosen so that warmup + steps steps take about `seconds`.  Returns
+    (Gcell-updates/s, record)."""
     import numpy as np
 
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     import oracle as O
 
     O.build(ref=False)
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    kz = 4
+    lib, _ = O._lib("port")
+    threads = int(lib.oracle_omp_threads())
     dx = (1.0 / n,) * 3
+    kz = min(n, max(CPU_SLAB_PLANES, 2 * threads))
     prim = O.random_prim(n + 2, n + 2, kz + 2, seed=0)
     cons = O.prim_to_cons(prim, GAMMA)
-    t0 = time.perf_counter()
-    O.simulate(prim, cons, GAMMA, dx, CFL, 1)
-    one = time.perf_counter() - t0
-    steps = max(1, int(seconds / max(one, 1e-6)))
+    if steps is None:
+        t0 = time.perf_counter()
+        O.simulate(prim, cons, GAMMA, dx, CFL, 1)
+        per_step = max(time.perf_counter() - t0, 1e-6)
+        warmup = max(warmup - 1, 0)
+        steps = max(3, int(seconds / per_step) - warmup - 1)
+    O.simulate(prim, cons, GAMMA, dx, CFL, warmup)
     t0 = time.perf_counter()
     O.simulate(prim, cons, GAMMA, dx, CFL, steps)
     el = time.perf_counter() - t0
-    cells = n * n * kz * steps
-    return {
-        "value": cells / el / 1e9,
-        "unit": UNIT,
-        "cores": cores,
-        "kind": "port",
-        "sample": f"{steps} steps of the reference loop (time_step, godunov, cons_to_prim) on a "
-                  f"{n}x{n}x{kz}-interior slab of the same random state, {el:.1f} s",
-        "_np": np.__version__,
-    }
+    value = n * n * kz * steps / el / 1e9
+    rec = {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+           "omp_threads": threads, "host_cpus": cores, "timed_s": el, "steps": steps, "slab_planes": kz,
+           "sample": f"{steps} timed steps of the reference loop (time_step, godunov, cons_to_prim) after "
+                     f"warm-up, on a {n}x{n}x{kz}-interior slab of the {n}^3 workload's random state, "
+                     f"{el:.1f} s, {threads} OpenMP threads",
+           "numpy": np.__version__}
+    return value, rec
+
+
+def cpu_baseline(n: int, seconds: float):
+    """The cpu_baseline leg of the GPU arm: the shared CPU sampler with one
+    warm-up step and as many timed steps as fill `seconds`."""
+    _, rec = cpu_loop_sample(n, seconds, 1)
+    return rec
 
 
 def run_reference(args):
     """The reference arm: the reference's CPU implementation of the path (the
     oracle port: the reference's own sources are not present where this runs)
     on all host cores.  A step is one step of the reference loop (time_step,
-    godunov, cons_to_prim) on an n x n x kz-interior slab of the same random
-    state, kz sized so that --warmup + --steps steps take about --cpu-seconds.
-    Under torchrun only rank 0 works and prints; the other ranks exit 0."""
-    import numpy as np
-
+    godunov, cons_to_prim) on a slab of the same random state, through the
+    shared CPU sampler, sized so that --warmup + --steps steps take about
+    --cpu-seconds.  Under torchrun only rank 0 works and prints; the other
+    ranks exit 0."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    import oracle as O
-
-    O.build(ref=False)
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     n = args.n
-    dx = (1.0 / n,) * 3
-    probe = O.random_prim(n + 2, n + 2, 3, seed=0)
-    pc = O.prim_to_cons(probe, GAMMA)
-    t0 = time.perf_counter()
-    O.simulate(probe, pc, GAMMA, dx, CFL, 1)
-    per_plane = max(time.perf_counter() - t0, 1e-6)
-    nsteps = args.warmup + args.steps
-    kz = int(max(1, min(n, args.cpu_seconds / nsteps / per_plane)))
-    prim = O.random_prim(n + 2, n + 2, kz + 2, seed=0)
-    cons = O.prim_to_cons(prim, GAMMA)
-    O.simulate(prim, cons, GAMMA, dx, CFL, args.warmup)
-    t0 = time.perf_counter()
-    O.simulate(prim, cons, GAMMA, dx, CFL, args.steps)
-    el = time.perf_counter() - t0
-    value = n * n * kz * args.steps / el / 1e9
-    sample = (f"{args.steps} timed steps (after {args.warmup} warm-up) of the reference loop on a "
-              f"{n}x{n}x{kz}-interior slab of the {n}^3 workload's random state, {el:.1f} s")
+    value, rec = cpu_loop_sample(n, args.cpu_seconds, args.warmup, args.steps)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": rec["timed_s"] * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"fused Euler step, {n}^3 interior, seeded random state (rho, p log-uniform "
                                "[0.1,10], u ~ N(0,1)), gamma 1.4, CFL 0.4", "n": n,
                    "l2": "CPU run (no GPU caches involved)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
-                         "numpy": np.__version__},
+        "cpu_baseline": rec,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference arm: the reference's CPU implementation of the path, as the oracle port (the "
-                "reference sources are not present where this runs); OpenMP over all host cores",
+                "reference sources are not present where this runs); OpenMP over all host cores, the same "
+                "sampler as the GPU arm's cpu_baseline leg",
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -9,6 +9,9 @@
 #include <float.h>
 #include <math.h>
 #include <stddef.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "euler_oracle.h"
 
@@ -35,3 +38,13 @@
 #undef SQRT
 #undef FABS
 #undef REAL_MAX
+
+/* The number of OpenMP threads a parallel region of this library uses. */
+int oracle_omp_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -30,6 +30,8 @@ EULER_ORACLE_DECLARE(f32, float)
 
 #undef EULER_ORACLE_DECLARE
 
+int oracle_omp_threads(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,8 +53,10 @@ static inline REAL FN(ke_prim)(PRIM_T q)
     return q.d * ((q.u[0] * q.u[0]) + (q.u[1] * q.u[1]) + (q.u[2] * q.u[2])) / (REAL)2;
 }
 
-/* hllc::operator(), hllc.hpp:50-105, for normal direction dir. */
-static FLUX_T FN(hllc)(int dir, REAL gamma, PRIM_T qL, PRIM_T qR)
+/* hllc::operator(), hllc.hpp:50-105, for normal direction dir.  Always
+ * inlined, so that with the direction loop unrolled dir is a constant at each
+ * call, as the reference's dir_t<D> tag makes it (hllc.hpp:52-53). */
+static inline __attribute__((always_inline)) FLUX_T FN(hllc)(int dir, REAL gamma, PRIM_T qL, PRIM_T qR)
 {
     REAL const un_L = qL.u[dir];
     REAL const un_R = qR.u[dir];
@@ -220,7 +222,10 @@ REAL FN(oracle_time_step)(REAL const* const* prim, int n0, int n1, int n2, REAL 
 }
 
 /* godunov, godunov.hpp:15-92: interior cells [1, n-1)^3, two HLLC solves per
- * axis per cell, cons updated in place from read-only prim. */
+ * axis per cell, cons updated in place from read-only prim.  The (k, j) rows
+ * are shared among the threads, as Kokkos's OpenMP MDRangePolicy tiles more
+ * than one axis (godunov.hpp:34-43), so a slab a few planes deep still keeps
+ * every core busy; cells are independent, so the split changes no bit. */
 void FN(oracle_godunov)(
         REAL const* const* prim,
         REAL* const* cons,
@@ -236,13 +241,14 @@ void FN(oracle_godunov)(
     REAL const ds[3] = {dx1 * dx2, dx2 * dx0, dx0 * dx1}; /* uniform_mesh.hpp:33-46 */
     REAL const dtodv = dt / (dx0 * dx1 * dx2);          /* uniform_mesh.hpp:48-51 */
     ptrdiff_t const stride[3] = {1, (ptrdiff_t)n0, (ptrdiff_t)n0 * (ptrdiff_t)n1};
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for collapse(2) schedule(static)
     for (int k = 1; k < n2 - 1; ++k) {
         for (int j = 1; j < n1 - 1; ++j) {
             for (int i = 1; i < n0 - 1; ++i) {
                 size_t const c = (size_t)i + (size_t)n0 * ((size_t)j + (size_t)n1 * (size_t)k);
                 PRIM_T const qc = FN(load_prim)(prim, c);
                 REAL acc[5] = {0, 0, 0, 0, 0};
+#pragma GCC unroll 3
                 for (int dir = 0; dir < 3; ++dir) {
                     PRIM_T const qL = FN(load_prim)(prim, c - (size_t)stride[dir]);
                     PRIM_T const qR = FN(load_prim)(prim, c + (size_t)stride[dir]);

@@ -11,7 +11,8 @@
 //   KOKKOS_FUNCTION / KOKKOS_LAMBDA, DefaultExecutionSpace::fence, ScopeGuard,
 //   and a declaration of submdspan (used only by uninstantiated templates).
 // Iteration order follows Iterate::Left (i fastest).  OpenMP splits the
-// outermost index; the only reduction is an exact min, so results do not
+// (k, j) rows among the threads, as Kokkos's OpenMP MDRangePolicy tiles more
+// than the outermost axis; the only reduction is an exact min, so results do not
 // depend on the thread count.
 #pragma once
 
@@ -307,7 +308,7 @@ template <class RankT, class IndexT, class F>
 void parallel_for(std::string const& /*label*/, MDRangePolicy<RankT, IndexT> const& p, F const& f)
 {
     using I = typename IndexT::type;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for collapse(2) schedule(static)
     for (std::int64_t k = p.begin[2]; k < p.end[2]; ++k) {
         for (std::int64_t j = p.begin[1]; j < p.end[1]; ++j) {
             for (std::int64_t i = p.begin[0]; i < p.end[0]; ++i) {
@@ -329,7 +330,7 @@ void parallel_reduce(
 #pragma omp parallel
     {
         T local = std::numeric_limits<T>::max();
-#pragma omp for schedule(static)
+#pragma omp for collapse(2) schedule(static)
         for (std::int64_t k = p.begin[2]; k < p.end[2]; ++k) {
             for (std::int64_t j = p.begin[1]; j < p.end[1]; ++j) {
                 for (std::int64_t i = p.begin[0]; i < p.end[0]; ++i) {
