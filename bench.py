@@ -75,6 +75,9 @@ def parse():
     ap.add_argument("--no-ops", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-fp32c", action="store_true")
+    ap.add_argument("--fp32c-implosion-n", type=int, default=256,
+                    help="interior cells per axis of the FP32c error run (implosion); 0 skips it")
+    ap.add_argument("--fp32c-implosion-steps", type=int, default=1000)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-grids", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=200)
@@ -88,7 +91,9 @@ def parse():
     ap.add_argument("--adj-n", type=int, default=128)
     ap.add_argument("--adj-steps", type=int, default=400)
     ap.add_argument("--adj-every", type=int, default=20)
-    ap.add_argument("--adj-dirs", type=int, default=4)
+    ap.add_argument("--adj-dirs", type=int, default=16)
+    ap.add_argument("--adj-smooth-dirs", type=int, default=8,
+                    help="central-difference directions of the smooth-state check (64^3, 50 steps); 0 skips it")
     return ap.parse_args()
 
 
@@ -343,6 +348,43 @@ def run_fp32c_leg(torch, E, args, stream, n0, dx, interior, steps_total, prim_re
     return out
 
 
+def implosion_precision(torch, E, stream, n, steps, precisions):
+    """The implosion (init_implode, n^3 interior, CFL 0.4) advanced `steps`
+    steps in FP64 and in each FP32 state of `precisions`: the FP32 states'
+    L1/Linf errors of rho, p and |u| against the FP64 run, their run times
+    and final times."""
+    n0 = n + 2
+    dx = (1.0 / n,) * 3
+    rec = {"n": n, "steps": steps}
+    with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, precision="f64", stream=stream) as sim:
+        sim.init_implode()
+        t0 = time.perf_counter()
+        sim.advance(steps)
+        torch.cuda.synchronize()
+        rec["f64_seconds"] = time.perf_counter() - t0
+        ref = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
+        sim.get_state(prim=ref)
+        rec["t_final"] = sim.time()[0]
+        rec["f64_totals"] = sim.totals()
+    torch.cuda.empty_cache()
+    for precision in precisions:
+        with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, precision=precision, stream=stream) as sim:
+            sim.init_implode()
+            t0 = time.perf_counter()
+            sim.advance(steps)
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
+            got = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
+            sim.get_state(prim=got)
+            rec[precision] = {"seconds": el, "t_final": sim.time()[0], "status": sim.status(),
+                              "totals": sim.totals(), "errors": state_errors(torch, got, ref)}
+            del got
+        torch.cuda.empty_cache()
+    del ref
+    torch.cuda.empty_cache()
+    return rec
+
+
 def run_precision_study(args):
     """Implosion (init_implode) at each N for study-steps steps: FP32 states
     against the plain FP64 run, L1/Linf of rho, p, |u|."""
@@ -354,38 +396,8 @@ def run_precision_study(args):
     E.load()
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    results = []
     for n in args.study_n:
-        n0 = n + 2
-        dx = (1.0 / n,) * 3
-        rec = {"n": n, "steps": args.study_steps}
-        with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, precision="f64", stream=stream) as sim:
-            sim.init_implode()
-            t0 = time.perf_counter()
-            sim.advance(args.study_steps)
-            torch.cuda.synchronize()
-            rec["f64_seconds"] = time.perf_counter() - t0
-            ref = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
-            sim.get_state(prim=ref)
-            rec["t_final"] = sim.time()[0]
-            rec["f64_totals"] = sim.totals()
-        torch.cuda.empty_cache()
-        for precision in ("f32c", "f32c_hilo", "f32"):
-            with E.Simulation(n0, n0, n0, GAMMA, dx, CFL, precision=precision, stream=stream) as sim:
-                sim.init_implode()
-                t0 = time.perf_counter()
-                sim.advance(args.study_steps)
-                torch.cuda.synchronize()
-                el = time.perf_counter() - t0
-                got = torch.empty((5, n0, n0, n0), dtype=torch.float64, device="cuda")
-                sim.get_state(prim=got)
-                rec[precision] = {"seconds": el, "t_final": sim.time()[0], "status": sim.status(),
-                                  "totals": sim.totals(), "errors": state_errors(torch, got, ref)}
-                del got
-            torch.cuda.empty_cache()
-        del ref
-        torch.cuda.empty_cache()
-        results.append(rec)
+        rec = implosion_precision(torch, E, stream, n, args.study_steps, ("f32c", "f32c_hilo", "f32"))
         print(json.dumps({"precision_study": rec}), flush=True)
     return 0
 
@@ -412,14 +424,93 @@ def box_weight_device(torch, nx):
     return w.cuda()
 
 
+def smooth_prim_device(torch, nx):
+    """A smooth, subsonic, everywhere-moving state on an nx^3 interior (ghosts
+    included), away from every kink of the HLLC flux: each normal velocity
+    rises strictly along its own axis, the sound speed rises strictly along
+    every axis, every velocity is positive and well below the sound speed."""
+    n = nx + 2
+    x = (torch.arange(n, dtype=torch.float64) - 1 + 0.5) / nx
+    X, Y, Z = x[None, None, :], x[None, :, None], x[:, None, None]
+    s = (X + Y + Z) / 3
+    prim = torch.empty((5, n, n, n), dtype=torch.float64)
+    prim[0] = 1.0 - 0.1 * s
+    prim[1] = 1.0 + 0.3 * s
+    prim[2] = (0.3 + 0.2 * X).expand(n, n, n)
+    prim[3] = (0.2 + 0.15 * Y).expand(n, n, n)
+    prim[4] = (0.25 + 0.1 * Z).expand(n, n, n)
+    return prim.cuda()
+
+
+def central_differences(torch, E, stream, prim0, w, dts, g0, ndirs, seed, eps=1e-6):
+    """Central differences of J = sum(rho(T) w) of the FP64 solver on the
+    fixed dt sequence, at eps and 2 eps, along seeded random (rho, p)
+    directions, beside the adjoint's <g0, v>."""
+    import numpy as np
+
+    n = prim0.shape[-1]
+    nx = n - 2
+    rng = np.random.default_rng(seed)
+    rows = []
+    with E.Simulation(n, n, n, GAMMA, (1.0 / nx,) * 3, CFL, stream=stream) as sim:
+        sim.set_dt_sequence(dts)
+        p = torch.empty_like(prim0)
+
+        def J_at(x):
+            sim.set_prim(x.contiguous())
+            sim.advance(len(dts))
+            sim.get_state(prim=p)
+            return float((p[0] * w).sum())
+
+        for _ in range(ndirs):
+            v = torch.zeros_like(prim0)
+            v[0] = torch.from_numpy(rng.normal(size=(n, n, n))).cuda()
+            v[1] = torch.from_numpy(rng.normal(size=(n, n, n))).cuda()
+            fd = {}
+            for h in (eps, 2 * eps):
+                fd[h] = (J_at(prim0 + h * v) - J_at(prim0 - h * v)) / (2 * h)
+            rows.append({"adjoint": float((g0 * v).sum()), "fd": fd[eps], "fd_2eps": fd[2 * eps],
+                         "richardson": 2 * fd[eps] - fd[2 * eps]})
+    scale = float(np.sqrt(np.mean([r["adjoint"] ** 2 for r in rows])))
+    rel = [abs(r["fd"] - r["adjoint"]) / abs(r["adjoint"]) for r in rows]
+    rel_r = [abs(r["richardson"] - r["adjoint"]) / abs(r["adjoint"]) for r in rows]
+    return {"eps": eps, "directions": ndirs,
+            "max_rel_err": max(rel), "median_rel_err": float(np.median(rel)),
+            "max_err_over_rms": max(abs(r["fd"] - r["adjoint"]) for r in rows) / scale,
+            "richardson_max_rel_err": max(rel_r), "richardson_median_rel_err": float(np.median(rel_r)),
+            "richardson_max_err_over_rms": max(abs(r["richardson"] - r["adjoint"]) for r in rows) / scale,
+            "rows": rows}
+
+
+def run_smooth_fd(torch, E, stream, ndirs, nx=64, nsteps=50):
+    """The adjoint against central differences on a kink-free state (64^3,
+    50 CFL steps held fixed, J over [0.4, 0.6]^3): the adjoint's own error,
+    apart from the HLLC kinks of the differentiation workload."""
+    n = nx + 2
+    prim0 = smooth_prim_device(torch, nx)
+    w = box_weight_device(torch, nx)
+    adj = E.Adjoint(n, n, n, nsteps, gamma=GAMMA, dx=(1.0 / nx,) * 3, cfl=CFL, checkpoint_every=10, stream=stream)
+    out = torch.empty_like(prim0)
+    adj.forward(prim0, out=out)
+    dts = adj.dts()
+    gT = torch.zeros_like(prim0)
+    gT[0] = w
+    g0 = torch.empty_like(prim0)
+    adj.backward(gT, g0)
+    adj.close()
+    rec = central_differences(torch, E, stream, prim0, w, dts, g0, ndirs, seed=77)
+    rec["workload"] = (f"smooth subsonic state {nx}^3 (velocities and sound speed strictly monotone along each "
+                       f"axis: no HLLC kink), {nsteps} CFL steps held fixed; J = sum over [0.4,0.6]^3 of rho(T) dv")
+    rec["target"] = {"max_rel_err": 1e-6, "met": bool(rec["max_rel_err"] <= 1e-6)}
+    return rec
+
+
 def run_adjoint_leg(torch, E, stream, args, ndirs):
     """Differentiation workload: gradient of J = sum_box rho(T) dv with respect
     to the initial rho and p (128^3 implosion with density noise, 400 steps at
     the forward pass's CFL dt sequence held fixed, checkpoints every 20 steps),
     its cost against a plain forward step, and central differences
     (eps = 1e-6) of the FP64 solver along seeded random (rho, p) directions."""
-    import numpy as np
-
     nx, nsteps, every = args.adj_n, args.adj_steps, args.adj_every
     n = nx + 2
     dx = (1.0 / nx,) * 3
@@ -463,39 +554,10 @@ def run_adjoint_leg(torch, E, stream, args, ndirs):
     # has kinks exactly at the initial state (a gas at rest with uniform
     # pressure sits at ustar == 0 on every face), where a central difference
     # carries an O(eps) term; 2 FD(eps) - FD(2 eps) cancels it
-    eps = 1e-6
-    rng = np.random.default_rng(2024)
-    rows = []
-    with E.Simulation(n, n, n, GAMMA, dx, CFL, stream=stream) as sim:
-        sim.set_dt_sequence(dts)
-        p = torch.empty_like(prim0)
-
-        def J_at(x):
-            sim.set_prim(x.contiguous())
-            sim.advance(nsteps)
-            sim.get_state(prim=p)
-            return float((p[0] * w).sum())
-
-        for _ in range(ndirs):
-            v = torch.zeros_like(prim0)
-            v[0] = torch.from_numpy(rng.normal(size=(n, n, n))).cuda()
-            v[1] = torch.from_numpy(rng.normal(size=(n, n, n))).cuda()
-            fd = {}
-            for h in (eps, 2 * eps):
-                fd[h] = (J_at(prim0 + h * v) - J_at(prim0 - h * v)) / (2 * h)
-            rows.append({"adjoint": float((g0 * v).sum()), "fd": fd[eps], "fd_2eps": fd[2 * eps],
-                         "richardson": 2 * fd[eps] - fd[2 * eps]})
-    if rows:
-        scale = float(np.sqrt(np.mean([r["adjoint"] ** 2 for r in rows])))
-        rel = [abs(r["fd"] - r["adjoint"]) / abs(r["adjoint"]) for r in rows]
-        rel_r = [abs(r["richardson"] - r["adjoint"]) / abs(r["adjoint"]) for r in rows]
-        rec["central_differences"] = {
-            "eps": eps, "directions": ndirs,
-            "max_rel_err": max(rel), "median_rel_err": float(np.median(rel)),
-            "max_err_over_rms": max(abs(r["fd"] - r["adjoint"]) for r in rows) / scale,
-            "richardson_max_rel_err": max(rel_r), "richardson_median_rel_err": float(np.median(rel_r)),
-            "richardson_max_err_over_rms": max(abs(r["richardson"] - r["adjoint"]) for r in rows) / scale,
-            "rows": rows}
+    if ndirs > 0:
+        rec["central_differences"] = central_differences(torch, E, stream, prim0, w, dts, g0, ndirs, seed=2024)
+    if args.adj_smooth_dirs > 0:
+        rec["smooth_state_central_differences"] = run_smooth_fd(torch, E, stream, args.adj_smooth_dirs)
     adj.close()
     return rec
 
@@ -695,10 +757,13 @@ def run_ours(args):
     peak = E.fma_rate("f64")
     props = torch.cuda.get_device_properties(local)
     nominal = 2 * 2 * props.multi_processor_count * 2.07e9  # 2 DFMA/clk/SM at the 2070 MHz max clock
-    roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak / 1e12,
-            "peak_source": "measured in this run: FP64 FMA probe (eulr_probe_fma_rate), FMA = 2 FLOP; "
-                           "the probe itself runs the FP64 pipe at ~84% of ncu's nominal 2 DFMA/clk/SM",
-            "peak_nominal": nominal / 1e12,
+    roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": nominal / 1e12,
+            "peak_source": "nominal FP64 rate: 2 DFMA/clk/SM (ncu's figure for this GPU), FMA = 2 FLOP, "
+                           f"{props.multi_processor_count} SMs at the 2070 MHz maximum clock (the clocks record "
+                           "shows the clock held during the timed region); MEASURED_PEAKS.json has no FP64 figure",
+            "peak_probe": peak / 1e12,
+            "peak_probe_source": "measured in this run: FP64 FMA probe (eulr_probe_fma_rate), a chain of "
+                                 "independent DFMAs; it reaches ~84% of the nominal rate",
             "kernel": "flux_tile_kernel<double, step>", "kernel_ms": flux_ms,
             "step_ms_sum_of_launches": step_ms_launches,
             "traffic": FLUX_F64_DRAM_BYTES_PER_CELL * interior,
@@ -708,6 +773,7 @@ def run_ours(args):
         fl = fpc["fused_step_fp64"] * interior
         roof["achieved"] = fl / (flux_ms * 1e-3) / 1e12
         roof["frac"] = roof["achieved"] / roof["peak"]
+        roof["frac_of_probe"] = roof["achieved"] / roof["peak_probe"]
         roof["flops_per_cell"] = fpc["fused_step_fp64"]
     else:
         roof["achieved"] = None
@@ -733,6 +799,21 @@ def run_ours(args):
         fp32c["speedup_vs_f64"] = fp32c["value"] / value
         del ref
         torch.cuda.empty_cache()
+        if args.fp32c_implosion_n > 0 and rank == 0:
+            # the stated error: the implosion after 1000 steps, FP32c against
+            # the plain FP64 run on the same grid
+            imp = implosion_precision(torch, E, stream, args.fp32c_implosion_n, args.fp32c_implosion_steps,
+                                      ("f32c",))
+            err = imp["f32c"]["errors"]
+            fp32c["errors_vs_f64_random_state"] = fp32c.pop("errors_vs_f64")
+            fp32c["errors_vs_f64_random_state_after_steps"] = fp32c.pop("errors_after_steps")
+            fp32c["errors_vs_f64"] = err
+            fp32c["errors_after_steps"] = imp["steps"]
+            fp32c["errors_workload"] = (f"init_implode {imp['n']}^3 interior, CFL 0.4, {imp['steps']} steps, "
+                                        "FP32c state against the plain FP64 run on the same grid")
+            fp32c["target"] = {"rho_l1_max": 1e-6, "speedup_min": 1.7,
+                               "met": bool(err["rho"]["l1"] <= 1e-6 and fp32c["speedup_vs_f64"] >= 1.7)}
+            fp32c["implosion"] = imp
 
     batch = None
     if not args.no_batch:
@@ -742,7 +823,7 @@ def run_ours(args):
     ops = None
     if not args.no_ops and rank == 0:
         prim = random_prim_device(torch, n0, n0, n0, seed=1)
-        ops = time_ops(torch, E, prim, n, fpc, peak, hbm_peak)
+        ops = time_ops(torch, E, prim, n, fpc, nominal, hbm_peak)
         del prim
         torch.cuda.empty_cache()
 

@@ -82,6 +82,31 @@ def test_random_operators_vs_oracle(cuda, euler, oracle_lib, shape):
     assert max(errs) <= TOL_F64_STEP, errs
 
 
+@pytest.mark.parametrize("shape", [(514, 20, 12), (515, 18, 10)], ids=["bench_pitch_514", "pitch_515"])
+def test_operators_at_bench_row_pitch(cuda, euler, oracle_lib, shape):
+    """The per-operator path at the benchmark's row length (514 cells per row,
+    dx = 1/512; and 515): prim_to_cons and time_step bit for bit, godunov to
+    1e-12 and its bit-identical variant bit for bit, against the oracle."""
+    O = oracle_lib
+    prim = O.random_prim(*shape, seed=515)
+    dx = (1 / 512,) * 3
+    g = 1.4
+    cons = O.prim_to_cons(prim, g)
+    dt = O.time_step(prim, g, dx)
+    ref = O.godunov(prim, cons, g, dx, 0.4 * dt)
+    pg = _t(cuda, prim)
+    cg = euler.prim_to_cons(pg, g)
+    assert np.array_equal(cg.cpu().numpy(), cons)
+    assert euler.time_step(pg, g, dx).item() == dt
+    ce = cg.clone()
+    euler.godunov(pg, cg, g, dx, 0.4 * dt)
+    errs = rel_linf(cg.cpu().numpy(), ref)
+    assert max(errs) <= TOL_F64_STEP, errs
+    euler.godunov(pg, ce, g, dx, 0.4 * dt, exact=True)
+    assert np.array_equal(ce.cpu().numpy(), ref)
+    assert np.array_equal(euler.cons_to_prim(cg, g).cpu().numpy(), O.cons_to_prim(cg.cpu().numpy(), g))
+
+
 @pytest.mark.parametrize("path", OPS, ids=os.path.basename)
 def test_exact_godunov_matches_reference_fixtures(cuda, euler, path):
     """The exact godunov against the fixtures made by the reference build

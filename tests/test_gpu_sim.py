@@ -83,6 +83,31 @@ def test_random_state_steps(cuda, euler, oracle_lib, shape):
         assert max(pe) <= tol and max(ce) <= tol, (steps, pe, ce)
 
 
+@pytest.mark.parametrize("shape", [(514, 20, 12), (515, 18, 10)], ids=["bench_pitch_514_tma", "pitch_515_plain"])
+def test_random_state_steps_at_bench_row_pitch(cuda, euler, oracle_lib, shape):
+    """The benchmark's row length: 514 cells per row (512 interior, dx =
+    1/512), an even n0 whose rows are staged by TMA at the full 4112-byte
+    pitch, and 515 (odd: plain loads).  Seeded random states as in the
+    benchmark, 1 and 5 steps against the oracle loop."""
+    O = oracle_lib
+    n0, n1, n2 = shape
+    dx = (1 / 512, 1 / 512, 1 / 512)
+    prim0 = O.random_prim(n0, n1, n2, seed=514)
+    for steps, tol in ((1, TOL_1), (5, 1e-11)):
+        p = prim0.copy()
+        c = O.prim_to_cons(p, 1.4)
+        t_ref = O.simulate(p, c, 1.4, dx, 0.4, steps)
+        with euler.Simulation(n0, n1, n2, 1.4, dx, 0.4) as sim:
+            sim.set_prim(prim0)
+            sim.advance(steps)
+            pg, cg = sim.state_numpy()
+            t, _, _ = sim.time()
+            assert sim.status() == 0
+        assert abs(t - t_ref) <= 1e-12 * t_ref
+        pe, ce = rel_linf(pg, p), rel_linf(cg, c)
+        assert max(pe) <= tol and max(ce) <= tol, (steps, pe, ce)
+
+
 def test_set_state_and_odd_step_counts(cuda, euler, oracle_lib):
     """advance() in uneven chunks (graph replays plus single steps) equals
     one long advance."""
