@@ -121,6 +121,29 @@ EulerConsArrays<Kokkos::mdspan<T const, Kokkos::extents<I, E0, E1, E2>, L>> as_c
     return as<Kokkos::mdspan<T const, Kokkos::extents<I, E0, E1, E2>, L>>(a);
 }
 
+// The same slices of every view of a bundle (euler_arrays.hpp:106-117,
+// 257-268): Kokkos::submdspan with an index, Kokkos::full_extent or a
+// [first, last) pair per axis.  A slice that keeps the leading axes, all
+// but the last of them whole, stays layout_left and can be passed to the
+// operators; any other is layout_stride.
+template <class E, class X, class L, class A, class... Slices>
+auto subspan(EulerPrimArrays<Kokkos::mdspan<E, X, L, A>> const& a, Slices const&... s)
+{
+    using V = decltype(Kokkos::submdspan(a.d, s...));
+    return EulerPrimArrays<V> {Kokkos::submdspan(a.d, s...), Kokkos::submdspan(a.p, s...),
+                               Kokkos::submdspan(a.ux0, s...), Kokkos::submdspan(a.ux1, s...),
+                               Kokkos::submdspan(a.ux2, s...)};
+}
+
+template <class E, class X, class L, class A, class... Slices>
+auto subspan(EulerConsArrays<Kokkos::mdspan<E, X, L, A>> const& a, Slices const&... s)
+{
+    using V = decltype(Kokkos::submdspan(a.d, s...));
+    return EulerConsArrays<V> {Kokkos::submdspan(a.d, s...), Kokkos::submdspan(a.e, s...),
+                               Kokkos::submdspan(a.mx0, s...), Kokkos::submdspan(a.mx1, s...),
+                               Kokkos::submdspan(a.mx2, s...)};
+}
+
 template <class E, class X, class L, class A>
 EulerPrimArrays<typename A::data_handle_type> data_handle(EulerPrimArrays<Kokkos::mdspan<E, X, L, A>> const& a) noexcept
 {

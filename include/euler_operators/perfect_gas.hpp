@@ -15,7 +15,7 @@ private:
     T m_gamma;
 
 public:
-    explicit PerfectGas(T const gamma) : m_gamma(gamma) {}
+    KOKKOS_FUNCTION explicit PerfectGas(T const gamma) : m_gamma(gamma) {}
 
     KOKKOS_FUNCTION T gamma() const noexcept { return m_gamma; }
 

@@ -10,7 +10,10 @@
 //     location the current device), so kernels and host code (the driver's
 //     NPY output, simulations/euler_simulation.cpp:71-79) can both read it;
 //   * DefaultExecutionSpace wraps a cudaStream_t (the legacy default stream
-//     unless constructed with one); fence() synchronises that stream.
+//     unless constructed with one); fence() synchronises that stream;
+//   * mdspan (layout_left, layout_right, layout_stride) with submdspan over
+//     index, full_extent and [first, last) pair slices, for the bundles'
+//     subspan helpers.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,11 +24,19 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <type_traits>
 #include <utility>
 
+// As with Kokkos's CUDA backend, KOKKOS_FUNCTION code is callable from the
+// device when nvcc compiles it.
+#if defined(__CUDACC__)
+#define KOKKOS_FUNCTION __host__ __device__
+#define KOKKOS_INLINE_FUNCTION __host__ __device__ inline
+#else
 #define KOKKOS_FUNCTION
 #define KOKKOS_INLINE_FUNCTION inline
+#endif
 
 namespace Kokkos {
 
@@ -43,15 +54,26 @@ public:
 
     constexpr extents() noexcept
     {
-        constexpr std::size_t se[] = {Exts...};
-        for (std::size_t r = 0; r < rank(); ++r) {
-            m_ext[r] = se[r] == dynamic_extent ? 0 : static_cast<IndexType>(se[r]);
+        if constexpr (sizeof...(Exts) > 0) {
+            constexpr std::size_t se[] = {Exts...};
+            for (std::size_t r = 0; r < rank(); ++r) {
+                m_ext[r] = se[r] == dynamic_extent ? 0 : static_cast<IndexType>(se[r]);
+            }
         }
     }
 
-    template <class... I, class = std::enable_if_t<sizeof...(I) == sizeof...(Exts)>>
+    template <class... I,
+              class = std::enable_if_t<sizeof...(I) == sizeof...(Exts) && (std::is_integral_v<I> && ...)>>
     constexpr explicit extents(I... e) noexcept : m_ext {static_cast<IndexType>(e)...}
     {
+    }
+
+    template <class OI>
+    constexpr explicit extents(std::array<OI, sizeof...(Exts)> const& e) noexcept
+    {
+        for (std::size_t r = 0; r < rank(); ++r) {
+            m_ext[r] = static_cast<IndexType>(e[r]);
+        }
     }
 
     template <class OI, std::size_t... OE>
@@ -89,6 +111,11 @@ struct layout_left
 struct layout_right
 {
 };
+// Any strides: what submdspan returns where a slice is not one contiguous
+// block of the parent.
+struct layout_stride
+{
+};
 
 template <class T>
 struct default_accessor
@@ -98,8 +125,10 @@ struct default_accessor
     using data_handle_type = T*;
 };
 
-// Non-owning multidimensional view over contiguous memory (host-side index
-// arithmetic only; the kernels receive data_handle() pointers).
+// Non-owning multidimensional view (host-side index arithmetic only; the
+// kernels receive data_handle() pointers).  layout_left and layout_right
+// views are contiguous, their strides follow from the extents; a
+// layout_stride view carries its own.
 template <class T, class Extents, class Layout = layout_right, class Accessor = default_accessor<T>>
 class mdspan
 {
@@ -113,21 +142,40 @@ public:
     using rank_type = typename Extents::rank_type;
     using data_handle_type = typename Accessor::data_handle_type;
     using reference = typename Accessor::reference;
+    using strides_type = std::array<index_type, Extents::rank()>;
 
     mdspan() = default;
 
-    template <class... I>
+    template <class... I, class = std::enable_if_t<(std::is_integral_v<I> && ...)>>
     mdspan(data_handle_type p, I... exts) noexcept : m_ptr(p), m_ext(exts...)
     {
+        static_assert(!std::is_same_v<Layout, layout_stride>, "a layout_stride view needs its strides");
+        set_contiguous_strides();
+    }
+
+    mdspan(data_handle_type p, Extents const& e) noexcept : m_ptr(p), m_ext(e)
+    {
+        static_assert(!std::is_same_v<Layout, layout_stride>, "a layout_stride view needs its strides");
+        set_contiguous_strides();
+    }
+
+    mdspan(data_handle_type p, Extents const& e, strides_type const& strides) noexcept
+        : m_ptr(p), m_ext(e), m_stride(strides)
+    {
+        static_assert(std::is_same_v<Layout, layout_stride>, "only a layout_stride view takes strides");
     }
 
     template <class OT, class OE, class OA>
     mdspan(mdspan<OT, OE, Layout, OA> const& o) noexcept : m_ptr(o.data_handle()), m_ext(o.extents())
     {
+        for (std::size_t r = 0; r < rank(); ++r) {
+            m_stride[r] = static_cast<index_type>(o.stride(r));
+        }
     }
 
     static constexpr rank_type rank() noexcept { return Extents::rank(); }
     index_type extent(rank_type r) const noexcept { return m_ext.extent(r); }
+    index_type stride(rank_type r) const noexcept { return m_stride[r]; }
     Extents const& extents() const noexcept { return m_ext; }
     data_handle_type data_handle() const noexcept { return m_ptr; }
 
@@ -144,29 +192,154 @@ public:
     reference operator()(I... idx) const noexcept
     {
         static_assert(sizeof...(I) == Extents::rank());
-        std::int64_t const ix[] = {static_cast<std::int64_t>(idx)...};
         std::int64_t off = 0;
-        if constexpr (std::is_same_v<Layout, layout_left>) {
-            for (std::size_t r = rank(); r-- > 0;) {
-                off = off * m_ext.extent(r) + ix[r];
-            }
-        } else {
+        if constexpr (sizeof...(I) > 0) {
+            std::int64_t const ix[] = {static_cast<std::int64_t>(idx)...};
             for (std::size_t r = 0; r < rank(); ++r) {
-                off = off * m_ext.extent(r) + ix[r];
+                off += ix[r] * static_cast<std::int64_t>(m_stride[r]);
             }
         }
         return m_ptr[off];
     }
 
 private:
+    void set_contiguous_strides() noexcept
+    {
+        index_type s = 1;
+        if constexpr (std::is_same_v<Layout, layout_left>) {
+            for (std::size_t r = 0; r < rank(); ++r) {
+                m_stride[r] = s;
+                s *= m_ext.extent(r);
+            }
+        } else {
+            for (std::size_t r = rank(); r-- > 0;) {
+                m_stride[r] = s;
+                s *= m_ext.extent(r);
+            }
+        }
+    }
+
     data_handle_type m_ptr = nullptr;
     Extents m_ext {};
+    strides_type m_stride {};
 };
 
-// Declared only: the reference's subspan helpers are templates nobody
-// instantiates in the operator path.
-template <class... Args>
-void submdspan(Args const&...) = delete;
+// Slice specifiers of submdspan: an index (the rank is dropped), full_extent,
+// or a half-open range [first, last) as a std::pair or a two-element
+// std::tuple.
+struct full_extent_t
+{
+    explicit full_extent_t() = default;
+};
+inline constexpr full_extent_t full_extent {};
+
+namespace detail {
+enum class slice_kind { index, full, range };
+
+template <class S>
+struct slice_traits
+{
+    static_assert(std::is_integral_v<S>, "a slice is an index, full_extent or a [first, last) pair");
+    static constexpr slice_kind kind = slice_kind::index;
+    template <class I>
+    static std::array<std::int64_t, 2> bounds(S const& s, I /*extent*/) noexcept
+    {
+        return {static_cast<std::int64_t>(s), 1};
+    }
+};
+
+template <>
+struct slice_traits<full_extent_t>
+{
+    static constexpr slice_kind kind = slice_kind::full;
+    template <class I>
+    static std::array<std::int64_t, 2> bounds(full_extent_t const&, I extent) noexcept
+    {
+        return {0, static_cast<std::int64_t>(extent)};
+    }
+};
+
+template <class A, class B>
+struct slice_traits<std::pair<A, B>>
+{
+    static constexpr slice_kind kind = slice_kind::range;
+    template <class I>
+    static std::array<std::int64_t, 2> bounds(std::pair<A, B> const& s, I /*extent*/) noexcept
+    {
+        return {static_cast<std::int64_t>(s.first), static_cast<std::int64_t>(s.second) - static_cast<std::int64_t>(s.first)};
+    }
+};
+
+template <class A, class B>
+struct slice_traits<std::tuple<A, B>>
+{
+    static constexpr slice_kind kind = slice_kind::range;
+    template <class I>
+    static std::array<std::int64_t, 2> bounds(std::tuple<A, B> const& s, I /*extent*/) noexcept
+    {
+        return {static_cast<std::int64_t>(std::get<0>(s)),
+                static_cast<std::int64_t>(std::get<1>(s)) - static_cast<std::int64_t>(std::get<0>(s))};
+    }
+};
+
+// Whether the slices of a layout_left view leave one contiguous block with
+// i fastest: the kept ranks come first, all but the last of them whole.
+// layout_right mirrors it (kept ranks last, all but the first whole).
+template <class... S>
+constexpr bool keeps_contiguous(bool left) noexcept
+{
+    constexpr slice_kind k[] = {slice_traits<S>::kind..., slice_kind::index};
+    constexpr std::size_t n = sizeof...(S);
+    std::size_t kept = 0;
+    for (std::size_t r = 0; r < n; ++r) {
+        kept += k[r] != slice_kind::index ? 1 : 0;
+    }
+    for (std::size_t q = 0; q < kept; ++q) {
+        std::size_t const r = left ? q : n - kept + q;
+        bool const edge = left ? q + 1 == kept : q == 0;
+        if (k[r] == slice_kind::index || (!edge && k[r] != slice_kind::full)) {
+            return false;
+        }
+    }
+    return true;
+}
+} // namespace detail
+
+// The part of a view that the slices select (C++26 std::submdspan,
+// restricted to the slice forms above); the result has dynamic extents.
+template <class T, class E, class L, class A, class... S>
+auto submdspan(mdspan<T, E, L, A> const& m, S const&... slices)
+{
+    static_assert(sizeof...(S) == E::rank(), "one slice per rank");
+    using I = typename E::index_type;
+    constexpr std::size_t rank_out = ((detail::slice_traits<S>::kind != detail::slice_kind::index ? 1 : 0) + ... + 0);
+    constexpr bool contiguous = (std::is_same_v<L, layout_left> && detail::keeps_contiguous<S...>(true))
+                                || (std::is_same_v<L, layout_right> && detail::keeps_contiguous<S...>(false));
+    using layout_out = std::conditional_t<contiguous, L, layout_stride>;
+    using extents_out = dextents<I, rank_out>;
+    std::array<I, rank_out> ext {};
+    std::array<I, rank_out> str {};
+    std::int64_t off = 0;
+    std::size_t r = 0;
+    std::size_t q = 0;
+    auto one = [&](auto const& s) {
+        using traits = detail::slice_traits<std::remove_cv_t<std::remove_reference_t<decltype(s)>>>;
+        std::array<std::int64_t, 2> const b = traits::bounds(s, m.extent(r));
+        off += b[0] * static_cast<std::int64_t>(m.stride(r));
+        if constexpr (traits::kind != detail::slice_kind::index) {
+            ext[q] = static_cast<I>(b[1]);
+            str[q] = m.stride(r);
+            ++q;
+        }
+        ++r;
+    };
+    (one(slices), ...);
+    if constexpr (contiguous) {
+        return mdspan<T, extents_out, layout_out, A>(m.data_handle() + off, extents_out(ext));
+    } else {
+        return mdspan<T, extents_out, layout_out, A>(m.data_handle() + off, extents_out(ext), str);
+    }
+}
 
 class DefaultExecutionSpace
 {

@@ -150,6 +150,24 @@ def godunov(prim: np.ndarray, cons: np.ndarray, gamma: float, dx, dt: float, imp
     return out
 
 
+def hllc_faces(direction: int, gamma: float, qL: np.ndarray, qR: np.ndarray, impl="port") -> np.ndarray:
+    """HLLC fluxes (d, e, m0, m1, m2) of faces normal to axis `direction`
+    between primitive states qL[k] and qR[k] (arrays of shape (N, 5): d, p,
+    u0, u1, u2), one call of the solver per face (hllc.hpp:50-105)."""
+    qL = np.ascontiguousarray(qL)
+    qR = np.ascontiguousarray(qR)
+    if qL.shape != qR.shape or qL.ndim != 2 or qL.shape[1] != 5 or qL.dtype != qR.dtype:
+        raise ValueError("face states are two arrays of shape (N, 5) of one dtype")
+    suf = _suffix(qL)
+    c = _DT[suf][1]
+    fn = _fn(impl, "hllc_face", suf)
+    out = np.empty_like(qL)
+    P = ctypes.POINTER(c)
+    for k in range(qL.shape[0]):
+        fn(int(direction), c(gamma), qL[k].ctypes.data_as(P), qR[k].ctypes.data_as(P), out[k].ctypes.data_as(P))
+    return out
+
+
 def simulate(prim: np.ndarray, cons: np.ndarray, gamma: float, dx, cfl: float, nsteps: int, impl="port"):
     """nsteps of the reference loop (euler_simulation.cpp:56-68), in place.
 

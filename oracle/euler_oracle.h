@@ -23,7 +23,8 @@ extern "C" {
     REAL oracle_step_##SUF(REAL* const* prim, REAL* const* cons, int n0, int n1, int n2, REAL gamma, REAL dx0, \
                            REAL dx1, REAL dx2, REAL cfl);                                        \
     void oracle_simulate_##SUF(REAL* const* prim, REAL* const* cons, int n0, int n1, int n2, REAL gamma,       \
-                               REAL dx0, REAL dx1, REAL dx2, REAL cfl, int nsteps, double* t_out);
+                               REAL dx0, REAL dx1, REAL dx2, REAL cfl, int nsteps, double* t_out);          \
+    void oracle_hllc_face_##SUF(int dir, REAL gamma, REAL const* qL, REAL const* qR, REAL* f);
 
 EULER_ORACLE_DECLARE(f64, double)
 EULER_ORACLE_DECLARE(f32, float)

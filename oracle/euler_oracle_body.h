@@ -95,6 +95,25 @@ static inline __attribute__((always_inline)) FLUX_T FN(hllc)(int dir, REAL gamma
     return f;
 }
 
+/* One HLLC face, for tests of other implementations of the solver: qL, qR
+ * are (d, p, u0, u1, u2), f receives (d, e, m0, m1, m2). */
+void FN(oracle_hllc_face)(int dir, REAL gamma, REAL const* qL, REAL const* qR, REAL* f)
+{
+    PRIM_T const a = {qL[0], qL[1], {qL[2], qL[3], qL[4]}};
+    PRIM_T const b = {qR[0], qR[1], {qR[2], qR[3], qR[4]}};
+    FLUX_T r;
+    switch (dir) {
+    case 0: r = FN(hllc)(0, gamma, a, b); break;
+    case 1: r = FN(hllc)(1, gamma, a, b); break;
+    default: r = FN(hllc)(2, gamma, a, b); break;
+    }
+    f[0] = r.d;
+    f[1] = r.e;
+    f[2] = r.m[0];
+    f[3] = r.m[1];
+    f[4] = r.m[2];
+}
+
 /* init_implode, init_implode.hpp:7-45.  Cell centres are evaluated in double
  * (the literal 0.5 promotes (i - 1) to double) and then rounded to REAL. */
 void FN(oracle_init_implode)(REAL* const* prim, int n0, int n1, int n2, REAL dx0, REAL dx1, REAL dx2)

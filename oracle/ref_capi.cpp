@@ -146,6 +146,28 @@ void simulate_t(
     }
 }
 
+// One face through the reference's own hllc functor (hllc.hpp:50-105).
+template <class T>
+void hllc_face_t(int dir, T g, T const* qL, T const* qR, T* f)
+{
+    PerfectGas<T> const eos(g);
+    EulerPrim<T> const a {.d = qL[0], .p = qL[1], .ux0 = qL[2], .ux1 = qL[3], .ux2 = qL[4]};
+    EulerPrim<T> const b {.d = qR[0], .p = qR[1], .ux0 = qR[2], .ux1 = qR[3], .ux2 = qR[4]};
+    EulerFlux<T> r {};
+    if (dir == 0) {
+        r = hllc()(dir_t<0>(), eos, a, b);
+    } else if (dir == 1) {
+        r = hllc()(dir_t<1>(), eos, a, b);
+    } else {
+        r = hllc()(dir_t<2>(), eos, a, b);
+    }
+    f[0] = r.d;
+    f[1] = r.e;
+    f[2] = r.mx0;
+    f[3] = r.mx1;
+    f[4] = r.mx2;
+}
+
 } // namespace
 
 extern "C" {
@@ -187,6 +209,10 @@ extern "C" {
             double* t_out)                                                                         \
     {                                                                                              \
         simulate_t<T>(prim, cons, n0, n1, n2, g, dx0, dx1, dx2, cfl, nsteps, t_out);               \
+    }                                                                                              \
+    void ref_hllc_face_##SUFFIX(int dir, T g, T const* qL, T const* qR, T* f)                      \
+    {                                                                                              \
+        hllc_face_t<T>(dir, g, qL, qR, f);                                                         \
     }
 
 EULER_REF_DEFINE(f64, double)
