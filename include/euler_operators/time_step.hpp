@@ -1,10 +1,14 @@
 // euler_operators drop-in for GB300: time_step, the reference's
 // euler_operators/time_step.hpp:8-41 -- min over all cells of
 // 1 / sum_d (c + |u_d|) / dx_d, without the CFL factor.  Reduced on the GPU by
-// eulr_time_step_{f64,f32} (bit-identical to the reference) into a
-// per-thread device scalar, then copied back: like the reference, it returns
-// a host value and therefore waits for the execution space's stream.
+// eulr_time_step_{f64,f32} (bit-identical to the reference) into a device
+// scalar of the calling thread on the current device (one per thread and
+// device, allocated on first use and kept until the process exits), then
+// copied back: like the reference, it returns a host value and therefore
+// waits for the execution space's stream.
 #pragma once
+
+#include <map>
 
 #include <euler_arrays.hpp>
 #include <euler_gb300_bridge.hpp>
@@ -21,10 +25,19 @@ T time_step(
 {
     namespace b = euler_gb300_bridge;
     using ty = b::types<T>;
-    static thread_local T* dt_dev = nullptr;
+    // the result slot of this thread on the current device: the reduction
+    // must write to memory of the device it runs on
+    static thread_local std::map<int, T*> dt_dev_of;
+    int dev = 0;
+    cudaError_t const de = cudaGetDevice(&dev);
+    if (de != cudaSuccess) {
+        throw std::runtime_error(std::string("time_step: ") + cudaGetErrorString(de));
+    }
+    T*& dt_dev = dt_dev_of[dev];
     if (dt_dev == nullptr) {
         cudaError_t const e = cudaMalloc(&dt_dev, sizeof(T));
         if (e != cudaSuccess) {
+            dt_dev = nullptr;
             throw std::runtime_error(std::string("time_step: ") + cudaGetErrorString(e));
         }
     }
