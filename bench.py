@@ -333,8 +333,9 @@ def run_fp32c_leg(torch, E, args, stream, n0, dx, interior, steps_total, prim_re
     del got
     torch.cuda.empty_cache()
     out = {"value": interior * args.steps / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms / args.steps,
-           "precision": "f32c: FP32 state, FP32 HLLC, compensated update (error-free sum of cell + six face "
-                        "terms, one rounding), FP64 internal energy for low-pressure cells",
+           "precision": "f32c: FP32 state, FP32 HLLC, compensated update (axis flux differences, TwoProduct "
+                        "and TwoSum into the cell with their errors folded back: one rounding at the state's "
+                        "scale), FP64 internal energy for low-pressure cells",
            "errors_vs_f64": err, "errors_after_steps": steps_total, "status": status,
            "roofline": {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes_per_cell": bytes_step / interior,
                         "achieved": bytes_step / (flux_ms * 1e-3) / 1e9, "peak": hbm_peak,

@@ -16,7 +16,8 @@ constexpr int kModeStepCons = 2; // fused step whose state is cons only (FP32): 
 
 // Update arithmetic of the fused FP32 step.
 constexpr int kCompNone = 0;  // plain: cons -= sum of the six face terms, FP32
-constexpr int kCompSum = 1;   // compensated: error-free sum of cons and the six terms, one rounding
+constexpr int kCompSum = 1;   // compensated: one rounding at the state's scale (column engine: axis
+                              // differences + TwoProduct/TwoSum; tile engine: error-free sum of six terms)
 constexpr int kCompHiLo = 2;  // compensated with a stored low word: cons = hi + lo (double-float)
 
 // Device scalars of a simulation.

@@ -218,9 +218,10 @@ typedef struct eulr_sim eulr_sim;
 
 typedef enum eulr_precision {
     EULR_PRECISION_F64 = 0,      /* plain FP64 */
-    EULR_PRECISION_F32C = 1,     /* FP32 state (4-byte words), FP32 fluxes, compensated update: the cell
-                                    and its six face terms are summed with error-free transformations and
-                                    rounded once; FP64 only for the internal energy of low-pressure cells */
+    EULR_PRECISION_F32C = 1,     /* FP32 state (4-byte words), FP32 fluxes, compensated update: the axis
+                                    flux differences times dt/dv ds are added to the cell by TwoProduct and
+                                    TwoSum with their errors folded back, one rounding at the state's
+                                    scale; FP64 only for the internal energy of low-pressure cells */
     EULR_PRECISION_F32 = 2,      /* plain FP32 (the reference's real_t = float) */
     EULR_PRECISION_F32C_HILO = 3 /* EULR_PRECISION_F32C with an FP32 low word per conservative field
                                     (double-float state, 8-byte words) */

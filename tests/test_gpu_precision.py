@@ -1,8 +1,9 @@
 """GPU tests of the FP32 simulation states against the FP64 oracle.
 
-EULR_PRECISION_F32C: FP32 state, compensated update (error-free sum of the
-cell and its six face terms, one rounding), FP64 internal energy for
-low-pressure cells.  EULR_PRECISION_F32C_HILO: the same with a stored FP32
+EULR_PRECISION_F32C: FP32 state, compensated update (the three axis flux
+differences times dt/dv ds, added to the cell by TwoProduct and TwoSum with
+their rounding errors folded back: one rounding at the state's scale), FP64
+internal energy for low-pressure cells.  EULR_PRECISION_F32C_HILO: the same with a stored FP32
 low word.  EULR_PRECISION_F32: plain FP32 (the reference's real_t = float),
 compared with the reference's own float loop as well.
 
