@@ -171,10 +171,28 @@ __device__ __forceinline__ T cell_invdt_exact(T d, T p, T u0, T u1, T u2, T gamm
 // e - |m|^2/(2 rho) has lost more than 8 of its 24 bits.
 constexpr float kLowPressure = 1.0f / 256.0f;
 
+// The FP64 internal energy of a low-pressure cell, (gamma-1) (e - |m|^2/(2 rho))
+// from the FP32 words (hi, plus the low words when the state stores them).
+// 1/rho is the FP32 reciprocal r refined by one Newton step in FP64
+// (relative error about 2^-44): no FP64 division routine.  Out of line: the
+// path is rare, and inlined its FP64 registers weigh on every cell's code.
+static __device__ __noinline__ float pressure_f64_rescue(float d, float e, float m0, float m1, float m2, float r, float gm1,
+                                                  const float* lo)
+{
+    double const dd = static_cast<double>(d) + (lo ? static_cast<double>(lo[0]) : 0.0);
+    double const ed = static_cast<double>(e) + (lo ? static_cast<double>(lo[1]) : 0.0);
+    double const a0 = static_cast<double>(m0) + (lo ? static_cast<double>(lo[2]) : 0.0);
+    double const a1 = static_cast<double>(m1) + (lo ? static_cast<double>(lo[3]) : 0.0);
+    double const a2 = static_cast<double>(m2) + (lo ? static_cast<double>(lo[4]) : 0.0);
+    double rd = static_cast<double>(r);
+    rd = rd * __fma_rn(-dd, rd, 2.0);
+    double const ke = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2) * rd;
+    return static_cast<float>(static_cast<double>(gm1) * (ed - ke));
+}
+
 // Pressure of an FP32 conservative state: the subtraction runs in FP32
 // unless the cell's internal energy is below kLowPressure of its total
-// energy, where it is redone in FP64 from the FP32 words (hi, plus the low
-// words when the state stores them).
+// energy, where it is redone in FP64 (pressure_f64_rescue).
 __device__ __forceinline__ float pressure_f32c(float d, float e, float m0, float m1, float m2, float r, float gm1,
                                                const float* lo)
 {
@@ -183,13 +201,7 @@ __device__ __forceinline__ float pressure_f32c(float d, float e, float m0, float
     if (eint > kLowPressure * e) {
         return gm1 * eint;
     }
-    double const dd = static_cast<double>(d) + (lo ? static_cast<double>(lo[0]) : 0.0);
-    double const ed = static_cast<double>(e) + (lo ? static_cast<double>(lo[1]) : 0.0);
-    double const a0 = static_cast<double>(m0) + (lo ? static_cast<double>(lo[2]) : 0.0);
-    double const a1 = static_cast<double>(m1) + (lo ? static_cast<double>(lo[3]) : 0.0);
-    double const a2 = static_cast<double>(m2) + (lo ? static_cast<double>(lo[4]) : 0.0);
-    double const ke = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2) / dd;
-    return static_cast<float>(static_cast<double>(gm1) * (ed - ke));
+    return pressure_f64_rescue(d, e, m0, m1, m2, r, gm1, lo);
 }
 
 // ------------------------------------------------------------------ HLLC
