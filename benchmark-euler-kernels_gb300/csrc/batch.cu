@@ -66,6 +66,8 @@ struct GridState {
     void* lo[2][5] = {};
     void* cs[2] = {};
     bool loaded = false;
+    int items = 0;          // work items of this grid in the current item list
+    bool ghost_fix = false; // FP64: copy 0 still holds the loaded ghost prim; fixed after the next step
 };
 
 constexpr int kKchunks[] = {8, 16, 32, 64};
@@ -85,15 +87,16 @@ struct eulr_batch {
     void* slab = nullptr;
     SimScalars* sc = nullptr;     // one per grid
     void* d_params[2] = {};       // FluxParams<T>[ngrids] per copy direction
-    void* d_ghost[2] = {};        // GhostParams<T>[ngrids] per copy direction
     int4* d_items = nullptr;      // work items (capacity: the smallest tiles and chunks)
     size_t item_capacity = 0;
     int nitems = 0;
     unsigned* d_head = nullptr;
+    unsigned* d_exited = nullptr; // CTAs of the running launch that found the queue empty
+    int* d_idle = nullptr;        // grids without interior cells, finalized by the launch's last CTA
+    int nidle = 0;
     int shape = 0;                // tile-shape variant of the batch kernel
     int kchunk = 32;
     int per_sm = 1;
-    int ghost_blocks = 1;
     int cur = 0;
     cudaGraphExec_t graph = nullptr;
     long long interior_cells = 0;
@@ -152,7 +155,6 @@ int upload_params(eulr_batch* b)
     for (int dir = 0; dir < 2; ++dir) {
         int const in = dir, out = 1 - dir;
         std::vector<FluxParams<T>> fp(n);
-        std::vector<GhostParams<T>> gp(n);
         for (int g = 0; g < n; ++g) {
             GridState const& G = b->grids[g];
             T const gamma = static_cast<T>(G.gamma);
@@ -189,31 +191,11 @@ int upload_params(eulr_batch* b)
             p.wmax = &b->sc[g].wmax;
             p.status = &b->sc[g].status;
             p.kchunk = b->kchunk;
+            p.fin = &b->sc[g];
+            p.grid_items = G.items;
             fp[g] = p;
-            GhostParams<T> q{};
-            q.g = G.g;
-            q.cons_in = cbundle_of<T>(G.cons[in]);
-            q.cons_out = bundle_of<T>(G.cons[out]);
-            if (b->comp == kCompHiLo) {
-                q.lo_in = cbundle_of<T>(G.lo[in]);
-                q.lo_out = bundle_of<T>(G.lo[out]);
-            }
-            if (is_f64(b)) {
-                q.prim_out = bundle_of<T>(G.prim[out]);
-                q.cs_out = static_cast<T*>(G.cs[out]);
-            }
-            q.comp = b->comp;
-            q.gamma = gamma;
-            q.gm1 = gamma - T(1);
-            q.invdx0 = ix0;
-            q.invdx1 = ix1;
-            q.invdx2 = ix2;
-            q.wmax = &b->sc[g].wmax;
-            gp[g] = q;
         }
         B_CUDA(cudaMemcpy(b->d_params[dir], fp.data(), sizeof(FluxParams<T>) * n, cudaMemcpyHostToDevice),
-               "upload batch parameters");
-        B_CUDA(cudaMemcpy(b->d_ghost[dir], gp.data(), sizeof(GhostParams<T>) * n, cudaMemcpyHostToDevice),
                "upload batch parameters");
     }
     return EULR_SUCCESS;
@@ -238,19 +220,24 @@ int build_items(eulr_batch* b, int shape, int kchunk)
         return b->grids[a].g.ncell() > b->grids[c].g.ncell();
     });
     std::vector<int4> items;
+    std::vector<int> idle;
     for (int g : order) {
         Geom const& G = b->grids[g].g;
         int const ix = G.n0 - 2, iy = G.n1 - 2, iz = G.n2 - 2;
-        if (ix <= 0 || iy <= 0 || iz <= 0) {
-            continue;
-        }
-        int const ntx = (ix + tx - 1) / tx, nty = (iy + ty - 1) / ty, nkc = (iz + kchunk - 1) / kchunk;
-        for (int kc = 0; kc < nkc; ++kc) {
-            for (int y = 0; y < nty; ++y) {
-                for (int x = 0; x < ntx; ++x) {
-                    items.push_back(make_int4(g, x, y, kc));
+        size_t const before = items.size();
+        if (ix > 0 && iy > 0 && iz > 0) {
+            int const ntx = (ix + tx - 1) / tx, nty = (iy + ty - 1) / ty, nkc = (iz + kchunk - 1) / kchunk;
+            for (int kc = 0; kc < nkc; ++kc) {
+                for (int y = 0; y < nty; ++y) {
+                    for (int x = 0; x < ntx; ++x) {
+                        items.push_back(make_int4(g, x, y, kc));
+                    }
                 }
             }
+        }
+        b->grids[g].items = static_cast<int>(items.size() - before);
+        if (b->grids[g].items == 0) {
+            idle.push_back(g);
         }
     }
     if (items.size() > b->item_capacity) {
@@ -260,6 +247,11 @@ int build_items(eulr_batch* b, int shape, int kchunk)
     if (!items.empty()) {
         B_CUDA(cudaMemcpy(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice),
                "upload work items");
+    }
+    b->nidle = static_cast<int>(idle.size());
+    if (!idle.empty()) {
+        B_CUDA(cudaMemcpy(b->d_idle, idle.data(), sizeof(int) * idle.size(), cudaMemcpyHostToDevice),
+               "upload idle grids");
     }
     b->shape = shape;
     b->kchunk = kchunk;
@@ -276,34 +268,91 @@ int build_items(eulr_batch* b, int shape, int kchunk)
     return EULR_SUCCESS;
 }
 
+// One step of every grid from copy `dir` to copy `1-dir`: ONE launch of the
+// persistent batch kernel.  Each grid's last work item finalizes that grid
+// (its next dt and clock), the launch's last CTA finalizes the grids without
+// interior cells and rewinds the queue.  Ghost layers are set at load
+// (prepare_grid) and, for the FP64 state, fixed once after the first step
+// (after_step).
 template <class T>
 int enqueue_step_t(eulr_batch* b, int dir)
 {
-    int const n = static_cast<int>(b->grids.size());
-    if (is_f64(b)) { // FP32 states: ghost layers set once at load (prepare_grid)
-        B_CUDA(launch_ghost_batch<T>(static_cast<GhostParams<T> const*>(b->d_ghost[dir]), n, b->ghost_blocks,
-                                     b->stream),
-               "batch ghost launch");
-    }
     BatchParams<T> bp{};
     bp.grids = static_cast<FluxParams<T> const*>(b->d_params[dir]);
     bp.items = b->d_items;
     bp.nitems = b->nitems;
     bp.head = b->d_head;
+    bp.exited = b->d_exited;
+    bp.idle = b->d_idle;
+    bp.nidle = b->nidle;
     long long grid = static_cast<long long>(b->sms) * b->per_sm;
     if (grid > b->nitems) {
         grid = b->nitems > 0 ? b->nitems : 1;
     }
     B_CUDA(launch_flux_batch<T>(b->shape, b->comp, &bp, static_cast<int>(grid), nullptr, b->stream),
            "batch flux launch");
-    B_CUDA(launch_finalize_batch<T>(b->sc, n, static_cast<T>(b->cfl), 1, b->d_head, b->stream),
-           "batch finalize launch");
     return EULR_SUCCESS;
 }
 
 int enqueue_step(eulr_batch* b, int dir)
 {
     return is_f64(b) ? enqueue_step_t<double>(b, dir) : enqueue_step_t<float>(b, dir);
+}
+
+// FP64 ghost layer of grid g from copy `in` to copy `out`: cons copied, prim
+// and sound speed rebuilt from cons (the reference's cons_to_prim over the
+// ghosts), their max wavespeed into the grid's ghost_wmax.
+int ghost_copy(eulr_batch* b, int g, int in, int out)
+{
+    GridState const& G = b->grids[g];
+    GhostParams<double> q{};
+    q.g = G.g;
+    q.cons_in = cbundle_of<double>(G.cons[in]);
+    q.cons_out = bundle_of<double>(G.cons[out]);
+    q.prim_out = bundle_of<double>(G.prim[out]);
+    q.cs_out = static_cast<double*>(G.cs[out]);
+    q.comp = kCompNone;
+    q.gamma = G.gamma;
+    q.gm1 = G.gamma - 1.0;
+    q.invdx0 = 1.0 / G.dx[0];
+    q.invdx1 = 1.0 / G.dx[1];
+    q.invdx2 = 1.0 / G.dx[2];
+    q.wmax = &b->sc[g].ghost_wmax;
+    B_CUDA(launch_ghost_shell<double>(q, b->sms, b->stream), "ghost shell");
+    return EULR_SUCCESS;
+}
+
+// After a step from copy `dir`: grids loaded since the previous step read
+// their loaded ghost prim in it; every later step reads the round trip, which
+// copy `dir` now takes from the copy the step wrote.
+int after_step(eulr_batch* b, int dir)
+{
+    for (int g = 0; g < static_cast<int>(b->grids.size()); ++g) {
+        if (b->grids[g].ghost_fix) {
+            B_TRY(ghost_copy(b, g, 1 - dir, dir));
+            b->grids[g].ghost_fix = false;
+        }
+    }
+    return EULR_SUCCESS;
+}
+
+bool ghost_fix_pending(eulr_batch const* b)
+{
+    for (GridState const& G : b->grids) {
+        if (G.ghost_fix) {
+            return true;
+        }
+    }
+    return false;
+}
+
+// One step launched directly (not from the graph), the copies swapped.
+int step_direct(eulr_batch* b)
+{
+    int const dir = b->cur;
+    B_TRY(enqueue_step(b, dir));
+    b->cur = 1 - dir;
+    return after_step(b, dir);
 }
 
 // dt of grid g's loaded state (copy 0), its clock and status zeroed.
@@ -319,6 +368,10 @@ int prepare_grid(eulr_batch* b, int g)
                                         b->sms, b->stream),
                "load");
         B_CUDA(launch_finalize_dt<double>(&b->sc[g], b->cfl, 0, b->stream), "finalize");
+        // copy 1's ghost layer once (after the first dt, which the loaded
+        // ghost prim sets); copy 0's follows after the first step
+        B_TRY(ghost_copy(b, g, 0, 1));
+        G.ghost_fix = true;
     } else {
         float const gm = static_cast<float>(G.gamma);
         B_CUDA(launch_invdt_max_cons(cbundle_of<float>(G.cons[0]), n, gm, 1.0f / static_cast<float>(G.dx[0]),
@@ -475,7 +528,6 @@ int eulr_batch_create(int precision, int ngrids, const eulr_grid_desc* grids, do
     b->grids.resize(ngrids);
     int const per_copy = is_f64(b) ? 11 : (b->comp == kCompHiLo ? 10 : 5);
     size_t bytes = 0;
-    long long max_shell = 1;
     size_t max_items = 0;
     for (int g = 0; g < ngrids; ++g) {
         eulr_grid_desc const& d = grids[g];
@@ -488,17 +540,15 @@ int eulr_batch_create(int precision, int ngrids, const eulr_grid_desc* grids, do
         bytes += 2 * per_copy * pad256(static_cast<size_t>(G.g.ncell()) * b->esize);
         long long const ix = std::max(d.n0 - 2, 0), iy = std::max(d.n1 - 2, 0), iz = std::max(d.n2 - 2, 0);
         b->interior_cells += ix * iy * iz;
-        max_shell = std::max(max_shell, G.g.ncell() - ix * iy * iz);
         // the most items any shape/chunk choice makes (8-wide tiles bound it)
         max_items += static_cast<size_t>((ix + 15) / 16) * ((iy + 7) / 8) * ((iz + 7) / 8);
     }
     b->item_capacity = max_items;
-    b->ghost_blocks = static_cast<int>(std::min<long long>((max_shell + 255) / 256, 64));
     size_t const scal = pad256(sizeof(SimScalars) * ngrids);
     size_t const pbytes = pad256(std::max(sizeof(FluxParams<double>), sizeof(FluxParams<float>)) * ngrids);
-    size_t const gbytes = pad256(std::max(sizeof(GhostParams<double>), sizeof(GhostParams<float>)) * ngrids);
     size_t const ibytes = pad256(sizeof(int4) * std::max<size_t>(max_items, 1));
-    size_t const total = bytes + scal + 2 * pbytes + 2 * gbytes + ibytes + 256;
+    size_t const idle_bytes = pad256(sizeof(int) * static_cast<size_t>(ngrids));
+    size_t const total = bytes + scal + 2 * pbytes + ibytes + idle_bytes + 256;
     e = cudaMalloc(&b->slab, total);
     if (e != cudaSuccess) {
         return bail(cfail(e, "cudaMalloc(batch state)"));
@@ -532,15 +582,16 @@ int eulr_batch_create(int precision, int ngrids, const eulr_grid_desc* grids, do
     for (int dir = 0; dir < 2; ++dir) {
         b->d_params[dir] = p;
         p += pbytes;
-        b->d_ghost[dir] = p;
-        p += gbytes;
     }
     b->d_items = reinterpret_cast<int4*>(p);
     p += ibytes;
+    b->d_idle = reinterpret_cast<int*>(p);
+    p += idle_bytes;
     b->d_head = reinterpret_cast<unsigned*>(p);
+    b->d_exited = b->d_head + 1;
     e = cudaMemset(b->sc, 0, scal);
     if (e == cudaSuccess) {
-        e = cudaMemset(b->d_head, 0, sizeof(unsigned));
+        e = cudaMemset(b->d_head, 0, 2 * sizeof(unsigned));
     }
     if (e != cudaSuccess) {
         return bail(cfail(e, "cudaMemset"));
@@ -669,7 +720,7 @@ int eulr_batch_autotune(eulr_batch* b, int trial_steps, int* shape_out, int* kch
     for (int g = 0; g < static_cast<int>(b->grids.size()); ++g) {
         B_TRY(prepare_grid(b, g));
     }
-    B_CUDA(cudaMemsetAsync(b->d_head, 0, sizeof(unsigned), b->stream), "cudaMemsetAsync");
+    B_CUDA(cudaMemsetAsync(b->d_head, 0, 2 * sizeof(unsigned), b->stream), "cudaMemsetAsync"); // head, exited
     B_CUDA(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
     if (shape_out != nullptr) {
         int tx = 0, ty = 0;
@@ -697,9 +748,12 @@ int eulr_batch_advance(eulr_batch* b, int nsteps)
         }
     }
     int left = nsteps;
+    if (left > 0 && ghost_fix_pending(b)) { // the first step after a load, then the ghost fix
+        B_TRY(step_direct(b));
+        --left;
+    }
     if (left > 0 && b->cur == 1) {
-        B_TRY(enqueue_step(b, 1));
-        b->cur = 0;
+        B_TRY(step_direct(b));
         --left;
     }
     if (left >= 2 && b->graph == nullptr) {
@@ -724,8 +778,7 @@ int eulr_batch_advance(eulr_batch* b, int nsteps)
         left -= 2;
     }
     if (left == 1) {
-        B_TRY(enqueue_step(b, 0));
-        b->cur = 1;
+        B_TRY(step_direct(b));
     }
     return EULR_SUCCESS;
 }

@@ -640,10 +640,12 @@ __global__ void __launch_bounds__(TX* TY) flux_tile_kernel(const __grid_constant
                 wait_slot<T, NSLOT>(c, s);
             }
         }
+        step_done(p); // the launch still counts this CTA, so the next launch starts from zero
         return;
     }
     if (MODE == kModeStep || MODE == kModeStepCons) {
         flush_wavespeed<T, TX * TY>(c, p.wmax, p.status);
+        step_done(p);
     }
 }
 
@@ -682,7 +684,9 @@ __global__ void __launch_bounds__(TX* TY) flux_batch_kernel(const __grid_constan
         T const k0 = dtodv * gp.ds0, k1 = dtodv * gp.ds1, k2 = dtodv * gp.ds2;
         tile_item<T, TX, TY, NSLOT, MODE, false, COMP>(c, gp, TmaMaps{}, k0, k1, k2, it.y, it.z, it.w);
         flush_wavespeed<T, NT>(c, gp.wmax, gp.status);
+        item_done(gp);
     }
+    batch_cta_done(b);
 }
 
 // Ghost shell of the step's output: cons copied, prim = cons_to_prim(cons)
@@ -798,55 +802,11 @@ __global__ void __launch_bounds__(256) ghost_shell_kernel(GhostParams<T> p)
     ghost_shell_body(p);
 }
 
-// Ghost shells of every grid of a batch: blockIdx.y selects the grid.
-template <class T>
-__global__ void __launch_bounds__(256) ghost_batch_kernel(const GhostParams<T>* gps)
-{
-    GhostParams<T> const p = gps[blockIdx.y];
-    ghost_shell_body(p);
-}
-
-// Turns the max-wavespeed accumulator into the next step's dt
-// (time_step.hpp:34-39: min over cells of 1/invdt == 1/max invdt), adds the
-// step just taken to the simulated time and clears the accumulator.
-template <class T>
-__device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time, const double* dt_seq = nullptr)
-{
-    if (add_time) {
-        // the step just taken, cfl*dt (or the fixed dt), added with separate
-        // roundings (no FMA) so every kernel that inlines this agrees bit for bit
-        double const step = dt_seq != nullptr ? dt_seq[s->steps]
-                                              : (sizeof(T) == 8 ? __dmul_rn(static_cast<double>(cfl), s->dt)
-                                                                : static_cast<double>(cfl * static_cast<T>(s->dt)));
-        s->t = __dadd_rn(s->t, step);
-        s->steps += 1;
-    }
-    unsigned long long const wk = s->wmax > s->ghost_wmax ? s->wmax : s->ghost_wmax;
-    T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(wk)));
-    T const dt = (m > T(0)) ? rcp_rn(m) : (sizeof(T) == 8 ? T(DBL_MAX) : T(FLT_MAX));
-    s->dt = static_cast<double>(dt);
-    s->wmax = 0ull;
-}
-
 template <class T>
 __global__ void finalize_dt_kernel(SimScalars* s, T cfl, int add_time, const double* dt_seq)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         finalize_one(s, cfl, add_time, dt_seq);
-    }
-}
-
-// Every grid of a batch, and the work-queue head back to zero for the next
-// launch of the batch kernel.
-template <class T>
-__global__ void finalize_batch_kernel(SimScalars* s, int ngrids, T cfl, int add_time, unsigned* head)
-{
-    int const g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g < ngrids) {
-        finalize_one(&s[g], cfl, add_time);
-    }
-    if (g == 0 && head != nullptr) {
-        *head = 0u;
     }
 }
 
@@ -991,27 +951,8 @@ cudaError_t launch_flux_batch(int shape, int comp, BatchParams<T> const* b, int 
     }
 }
 
-template <class T>
-cudaError_t launch_ghost_batch(GhostParams<T> const* gps, int ngrids, int blocks_per_grid, cudaStream_t s)
-{
-    dim3 grid(static_cast<unsigned>(blocks_per_grid), static_cast<unsigned>(ngrids));
-    ghost_batch_kernel<T><<<grid, 256, 0, s>>>(gps);
-    return cudaGetLastError();
-}
-
-template <class T>
-cudaError_t launch_finalize_batch(SimScalars* sc, int ngrids, T cfl, int add_time, unsigned* head, cudaStream_t s)
-{
-    finalize_batch_kernel<T><<<(ngrids + 255) / 256, 256, 0, s>>>(sc, ngrids, cfl, add_time, head);
-    return cudaGetLastError();
-}
-
 template cudaError_t launch_flux_batch<double>(int, int, BatchParams<double> const*, int, int*, cudaStream_t);
 template cudaError_t launch_flux_batch<float>(int, int, BatchParams<float> const*, int, int*, cudaStream_t);
-template cudaError_t launch_ghost_batch<double>(GhostParams<double> const*, int, int, cudaStream_t);
-template cudaError_t launch_ghost_batch<float>(GhostParams<float> const*, int, int, cudaStream_t);
-template cudaError_t launch_finalize_batch<double>(SimScalars*, int, double, int, unsigned*, cudaStream_t);
-template cudaError_t launch_finalize_batch<float>(SimScalars*, int, float, int, unsigned*, cudaStream_t);
 
 template <class T>
 struct FluxDispatch;

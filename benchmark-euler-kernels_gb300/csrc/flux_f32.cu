@@ -408,6 +408,7 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
                                 bad);
     }
     col_flush(sh, wmaxf, bad, p.wmax, p.status);
+    step_done(p);
 }
 
 // The column engine over a batch: CTAs pop (grid, tile x, tile y, chunk)
@@ -447,7 +448,9 @@ __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant_
             col_item<COMP, false>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
         }
         col_flush(sh, wmaxf, bad, gp.wmax, gp.status);
+        item_done(gp);
     }
+    batch_cta_done(b);
 }
 
 } // namespace f32col

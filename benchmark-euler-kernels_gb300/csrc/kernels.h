@@ -27,7 +27,8 @@ struct SimScalars {
     double t;                // simulated time: sum of cfl*dt over the steps taken
     long long steps;         // steps taken
     int status;              // bit 0: a cell became non-finite or non-physical
-    int pad;
+    unsigned done;           // CTAs (one grid) or work items (batch) of the running step that finished;
+                             // the last one finalizes the step and zeroes it
     unsigned long long ghost_wmax; // FP32 states: max invdt of the ghost layer, which never changes (set at load)
 };
 
@@ -62,6 +63,8 @@ struct FluxParams {
     int* status;              // step mode: set to 1 on a non-physical cell
     int tiles_x, tiles_y, kchunk, nwork; // work decomposition (kchunk <= 0: default)
     int per_sm;                          // resident CTAs per SM (from configure_flux)
+    SimScalars* fin;  // step mode, when set: the kernel finalizes the step itself (next dt, clock)
+    int grid_items;   // batch: work items of this grid in the current item list
 };
 
 // Launch parameters of the multi-grid batch kernel.
@@ -71,6 +74,9 @@ struct BatchParams {
     const int4* items;          // work items (grid, tile x, tile y, chunk), largest grids first
     int nitems;
     unsigned* head;             // work-queue head; zero before each launch
+    unsigned* exited;           // CTAs that found the queue empty; the last resets head and itself
+    const int* idle;            // grids without interior cells (no work item): finalized by the last CTA
+    int nidle;
 };
 
 template <class T>
@@ -127,10 +133,6 @@ int batch_shape_count();
 void batch_shape(int shape, int* tx, int* ty);
 template <class T>
 cudaError_t launch_flux_batch(int shape, int comp, BatchParams<T> const* b, int grid, int* per_sm, cudaStream_t s);
-template <class T>
-cudaError_t launch_ghost_batch(GhostParams<T> const* gps, int ngrids, int blocks_per_grid, cudaStream_t s);
-template <class T>
-cudaError_t launch_finalize_batch(SimScalars* sc, int ngrids, T cfl, int add_time, unsigned* head, cudaStream_t s);
 template <class T>
 cudaError_t launch_ghost_shell(GhostParams<T> p, int sms, cudaStream_t s);
 template <class T>

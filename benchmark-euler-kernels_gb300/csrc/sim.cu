@@ -9,12 +9,19 @@
 // instructions are stored rather than recomputed.  The FP32 states keep cons
 // only (plus 5 low-word fields for EULR_PRECISION_F32C_HILO): their step is
 // bound by HBM, so prim and the sound speed are rebuilt on chip.  One step reads copy
-// `cur` and writes copy `1-cur`:
-//   ghost_shell  -- out ghosts: cons copied, prim = cons_to_prim(cons)
-//                   (the reference runs cons_to_prim over ghosts too)
-//   flux (step)  -- out interior: HLLC update + cons_to_prim + sound speed,
-//                   and the max wavespeed of the new state
-//   finalize_dt  -- dt of the new state, simulated time += cfl*dt (FP64)
+// `cur` and writes copy `1-cur`, and is ONE launch of the fused step kernel:
+// the HLLC update, cons_to_prim and the sound speed of the interior, the max
+// wavespeed of the new state, and -- by the last CTA to finish -- the dt of
+// the new state and the simulated time (+= cfl*dt, FP64).
+// Ghost layers: the reference runs cons_to_prim over the ghosts every step
+// (cons_to_prim.hpp:26-27) while godunov never changes their cons, so from
+// the second step on every ghost prim is the round trip
+// cons_to_prim(prim_to_cons(loaded prim)), the same every step.  Loading
+// therefore writes copy 1's ghost layer once (cons copied, prim and sound
+// speed from cons, their max wavespeed kept in ghost_wmax, which every dt
+// includes); copy 0 keeps the loaded ghost prim for the first step and gets
+// the round trip once, right after it.  The recording steps of the adjoint
+// (a second prim output) still rebuild the output's ghost layer each step.
 // Two steps (A->B, B->A) are captured once into a CUDA graph and replayed.
 //
 // Precisions: EULR_PRECISION_F64 (FP64 state and arithmetic),
@@ -103,6 +110,7 @@ struct eulr_sim {
     long long dt_seq_len = 0;
     long long host_steps = 0;  // steps taken since the state was loaded (host-side count)
     double* rec[5] = {};       // set only inside sim_advance_recording: a second prim output
+    bool ghost_fix = false;    // FP64: copy 0 still holds the loaded ghost prim; fixed after the next step
 };
 
 namespace {
@@ -237,16 +245,19 @@ GhostParams<T> ghost_params(eulr_sim* s, int in, int out, unsigned long long* wm
     return gp;
 }
 
-// One fused step from copy `in` to copy `1-in`; with `ev` (4 events) the
-// launches are bracketed for per-kernel timing.  The ghost layer is rebuilt
-// every step for the FP64 state (the reference runs cons_to_prim over ghosts,
-// and the first step's ghost prim is the loaded one); the FP32 states' ghost
-// cons never change, so both copies get them once at load and the step
-// skips the ghost launch (its wavespeed is the stored ghost_wmax).
+// One fused step from copy `in` to copy `1-in`: one launch of the step
+// kernel, which also finalizes the step (next dt, clock).  With `ev` (4
+// events) the launches are bracketed for per-kernel timing (ghost layer,
+// step, finalize; the first and last are empty except when recording or on
+// grids without interior cells).  Ghost layers are set at load (see the top
+// of this file); recording steps rebuild the output's ghost layer, which
+// writes its prim into the recording too.  A grid without interior cells
+// launches no step kernel: a finalize launch takes its step.
 template <class T>
 int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
 {
     int const out = 1 - in;
+    bool const interior = s->g.n0 > 2 && s->g.n1 > 2 && s->g.n2 > 2;
     T const ix0 = T(1) / static_cast<T>(s->dx[0]);
     T const ix1 = T(1) / static_cast<T>(s->dx[1]);
     T const ix2 = T(1) / static_cast<T>(s->dx[2]);
@@ -255,7 +266,7 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[0], s->stream), "cudaEventRecord");
     }
-    if (is_f64(s)) {
+    if (is_f64(s) && s->rec[0] != nullptr) {
         SIM_CUDA(launch_ghost_shell<T>(ghost_params<T>(s, in, out, &s->sc->wmax), s->sms, s->stream),
                  "ghost shell launch");
     }
@@ -295,14 +306,20 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
     p.wmax = &s->sc->wmax;
     p.status = &s->sc->status;
     p.per_sm = s->per_sm;
+    p.fin = s->sc;
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[1], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_flux<T>(p, s->tma ? &s->maps[in] : nullptr, kModeStep, s->comp, s->sms, s->stream), "step launch");
+    if (interior) {
+        SIM_CUDA(launch_flux<T>(p, s->tma ? &s->maps[in] : nullptr, kModeStep, s->comp, s->sms, s->stream),
+                 "step launch");
+    }
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[2], s->stream), "cudaEventRecord");
     }
-    SIM_CUDA(launch_finalize_dt<T>(s->sc, static_cast<T>(s->cfl), 1, s->stream, s->dt_seq), "finalize launch");
+    if (!interior) {
+        SIM_CUDA(launch_finalize_dt<T>(s->sc, static_cast<T>(s->cfl), 1, s->stream, s->dt_seq), "finalize launch");
+    }
     if (ev != nullptr) {
         SIM_CUDA(cudaEventRecord(ev[3], s->stream), "cudaEventRecord");
     }
@@ -312,6 +329,41 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
 int enqueue_step(eulr_sim* s, int in, cudaEvent_t* ev = nullptr)
 {
     return is_f64(s) ? enqueue_step_t<double>(s, in, ev) : enqueue_step_t<float>(s, in, ev);
+}
+
+// FP64: copy 1 gets copy 0's ghost layer with its prim and sound speed
+// rebuilt from cons, and their max wavespeed goes to ghost_wmax (zero
+// before).  Copy 0 keeps its ghost prim until the first step has read it.
+int set_ghost_layer(eulr_sim* s)
+{
+    SIM_CUDA(launch_ghost_shell<double>(ghost_params<double>(s, 0, 1, &s->sc->ghost_wmax), s->sms, s->stream),
+             "ghost shell launch");
+    s->ghost_fix = true;
+    return EULR_SUCCESS;
+}
+
+// After a step: the first step since a load has read copy 0's loaded ghost
+// prim, which every later step replaces by the round trip; copy 0 takes it
+// from copy 1 now (same cons, same prim, the same wavespeeds again).
+int after_step(eulr_sim* s)
+{
+    if (s->ghost_fix) {
+        int const in = s->cur;     // the copy the step wrote
+        int const out = 1 - in;    // the copy it read
+        GhostParams<double> q = ghost_params<double>(s, in, out, &s->sc->ghost_wmax);
+        q.prim_rec = Bundle<double>{}; // a recording step has recorded its own ghost layer
+        SIM_CUDA(launch_ghost_shell<double>(q, s->sms, s->stream), "ghost shell launch");
+        s->ghost_fix = false;
+    }
+    return EULR_SUCCESS;
+}
+
+// One step launched directly (not from the graph), the copies swapped.
+int step_direct(eulr_sim* s, cudaEvent_t* ev = nullptr)
+{
+    SIM_TRY(enqueue_step(s, s->cur, ev));
+    s->cur = 1 - s->cur;
+    return after_step(s);
 }
 
 // After a state was loaded into copy 0: sound speed (FP64 state), dt of the
@@ -335,6 +387,7 @@ int prepare_loaded(eulr_sim* s, bool derive_cons = false)
                                           1.0 / s->dx[1], 1.0 / s->dx[2], &s->sc->wmax, s->sms, s->stream),
                  "load launch");
         SIM_CUDA(launch_finalize_dt<double>(s->sc, s->cfl, 0, s->stream), "finalize launch");
+        SIM_TRY(set_ghost_layer(s)); // after the first dt, which the loaded ghost prim sets
     } else {
         float const g = static_cast<float>(s->gamma);
         SIM_CUDA(launch_invdt_max_cons(cbundle_of<float>(s->cons[0]), ncell(s), g, 1.0f / static_cast<float>(s->dx[0]),
@@ -466,13 +519,11 @@ int sim_advance_recording(eulr_sim* s, double* const* dst)
         }
         s->rec[f] = dst[f];
     }
-    int const in = s->cur;
-    int const st = enqueue_step(s, in); // launched directly: the captured graph has no second output
+    int const st = step_direct(s); // launched directly: the captured graph has no second output
     for (int f = 0; f < 5; ++f) {
         s->rec[f] = nullptr;
     }
     SIM_TRY(st);
-    s->cur = 1 - in;
     s->host_steps += 1;
     return EULR_SUCCESS;
 }
@@ -491,8 +542,9 @@ int sim_restore(eulr_sim* s, const double* const* src, long long step)
     SimScalars h{};
     h.steps = step;
     SIM_CUDA(cudaMemcpyAsync(s->sc, &h, sizeof(h), cudaMemcpyHostToDevice, s->stream), "restore scalars");
-    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize"); // h is a stack value
     s->cur = 0;
+    SIM_TRY(set_ghost_layer(s));
+    SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize"); // h is a stack value
     s->host_steps = step;
     s->loaded = true;
     return EULR_SUCCESS;
@@ -696,9 +748,12 @@ int eulr_sim_advance(eulr_sim* s, int nsteps)
     }
     s->host_steps += nsteps;
     int left = nsteps;
+    if (left > 0 && s->ghost_fix) { // the first step after a load, then the ghost fix
+        SIM_TRY(step_direct(s));
+        --left;
+    }
     if (left > 0 && s->cur == 1) {
-        SIM_TRY(enqueue_step(s, 1));
-        s->cur = 0;
+        SIM_TRY(step_direct(s));
         --left;
     }
     if (left >= 2 && s->graph == nullptr) {
@@ -723,8 +778,7 @@ int eulr_sim_advance(eulr_sim* s, int nsteps)
         left -= 2;
     }
     if (left == 1) {
-        SIM_TRY(enqueue_step(s, 0));
-        s->cur = 1;
+        SIM_TRY(step_direct(s));
     }
     return EULR_SUCCESS;
 }
@@ -864,7 +918,8 @@ int eulr_sim_set_dt_sequence(eulr_sim* s, const double* dts, long long n)
 
 int eulr_sim_launches_per_step(eulr_sim* s)
 {
-    return (s != nullptr && !is_f64(s)) ? 2 : 3;
+    (void)s;
+    return 1;
 }
 
 int eulr_sim_profile_step(eulr_sim* s, float ms[3])
@@ -876,13 +931,16 @@ int eulr_sim_profile_step(eulr_sim* s, float ms[3])
     if (!s->loaded) {
         return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "no state loaded");
     }
+    if (s->dt_seq != nullptr && s->host_steps + 1 > s->dt_seq_len) {
+        return eulr::sim_fail(EULR_ERR_INVALID_ARGUMENT, "advance past the end of the fixed dt sequence");
+    }
     cudaEvent_t ev[4] = {};
     for (auto& e : ev) {
         SIM_CUDA(cudaEventCreate(&e), "cudaEventCreate");
     }
-    int st = enqueue_step(s, s->cur, ev);
+    int st = step_direct(s, ev);
     if (st == EULR_SUCCESS) {
-        s->cur = 1 - s->cur;
+        s->host_steps += 1;
         cudaError_t e = cudaEventSynchronize(ev[3]);
         for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
             e = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);

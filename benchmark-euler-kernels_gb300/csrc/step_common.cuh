@@ -5,6 +5,8 @@
 #include "euler_device.cuh"
 #include "kernels.h"
 
+#include <cfloat>
+
 namespace eulr {
 namespace {
 
@@ -80,6 +82,92 @@ __device__ __forceinline__ T dt_over_dv(FluxParams<T> const& p)
         return static_cast<T>((p.cfl * *p.dt_dev) / p.dv);
     }
     return p.dtodv;
+}
+
+// Turns the max-wavespeed accumulator into the next step's dt
+// (time_step.hpp:34-39: min over cells of 1/invdt == 1/max invdt), adds the
+// step just taken to the simulated time and clears the accumulator.  The
+// accumulator is read with a volatile load: other CTAs of the same launch
+// raised it by atomics, and a cached copy must not answer.
+template <class T>
+__device__ __forceinline__ void finalize_one(SimScalars* s, T cfl, int add_time, const double* dt_seq = nullptr)
+{
+    if (add_time) {
+        // the step just taken, cfl*dt (or the fixed dt), added with separate
+        // roundings (no FMA) so every kernel that inlines this agrees bit for bit
+        double const step = dt_seq != nullptr ? dt_seq[s->steps]
+                                              : (sizeof(T) == 8 ? __dmul_rn(static_cast<double>(cfl), s->dt)
+                                                                : static_cast<double>(cfl * static_cast<T>(s->dt)));
+        s->t = __dadd_rn(s->t, step);
+        s->steps += 1;
+    }
+    unsigned long long const w = *reinterpret_cast<volatile unsigned long long*>(&s->wmax);
+    unsigned long long const wk = w > s->ghost_wmax ? w : s->ghost_wmax;
+    T const m = static_cast<T>(__longlong_as_double(static_cast<long long>(wk)));
+    T const dt = (m > T(0)) ? rcp_rn(m) : (sizeof(T) == 8 ? T(DBL_MAX) : T(FLT_MAX));
+    s->dt = static_cast<double>(dt);
+    s->wmax = 0ull;
+}
+
+// The step's own finalize, so that a step is one launch.  Called by thread 0
+// of every CTA of a single-grid step launch after its wavespeed flush (the
+// atomicMax precedes it in the same thread): the fence orders that flush
+// before the count, and the CTA that counts last -- every other CTA has
+// flushed and read this step's dt by then -- finalizes the step and rewinds
+// the counter for the next launch.
+template <class T>
+__device__ __forceinline__ void step_done(FluxParams<T> const& p)
+{
+    if (p.fin == nullptr || threadIdx.x != 0) {
+        return;
+    }
+    __threadfence();
+    if (atomicAdd(&p.fin->done, 1u) == gridDim.x - 1) {
+        __threadfence();
+        finalize_one(p.fin, static_cast<T>(p.cfl), 1, p.dt_seq);
+        p.fin->done = 0u;
+    }
+}
+
+// The same for one work item of a batch launch: the grid's last item to
+// finish finalizes that grid (its items were all taken from the queue before,
+// so no CTA reads the grid's dt afterwards in this launch).  Thread 0, after
+// the item's flush.
+template <class T>
+__device__ __forceinline__ void item_done(FluxParams<T> const& gp)
+{
+    if (gp.fin == nullptr || threadIdx.x != 0) {
+        return;
+    }
+    __threadfence();
+    if (atomicAdd(&gp.fin->done, 1u) == static_cast<unsigned>(gp.grid_items) - 1u) {
+        __threadfence();
+        finalize_one(gp.fin, static_cast<T>(gp.cfl), 1, gp.dt_seq);
+        gp.fin->done = 0u;
+    }
+}
+
+// A batch CTA leaving (the queue is empty for it).  Thread 0.  The last CTA
+// to leave rewinds the queue head for the next launch -- every CTA has made
+// its last pop by then -- and finalizes the grids that have no work item.
+template <class T>
+__device__ __forceinline__ void batch_cta_done(BatchParams<T> const& b)
+{
+    if (b.exited == nullptr || threadIdx.x != 0) {
+        return;
+    }
+    __threadfence();
+    if (atomicAdd(b.exited, 1u) == gridDim.x - 1) {
+        __threadfence();
+        for (int i = 0; i < b.nidle; ++i) {
+            FluxParams<T> const& g = b.grids[b.idle[i]];
+            if (g.fin != nullptr) {
+                finalize_one(g.fin, static_cast<T>(g.cfl), 1, g.dt_seq);
+            }
+        }
+        *b.head = 0u;
+        *b.exited = 0u;
+    }
 }
 
 // Chunk length (planes per work item) that balances the persistent grid:

@@ -273,13 +273,19 @@ int eulr_sim_time(eulr_sim* sim, double* t, double* next_dt, long long* steps);
  * or non-positive density/pressure; waits for the stream. */
 int eulr_sim_status(eulr_sim* sim);
 
-/* Number of kernel launches one step issues (for launch accounting). */
+/* Number of kernel launches one step issues (for launch accounting): 1, the
+ * fused step kernel, which also turns the new state's max wavespeed into the
+ * next dt (its last CTA).  Two one-off launches are not counted: the ghost
+ * layer of the second state copy at load, and of the first copy after the
+ * first step since a load (FP64 states). */
 int eulr_sim_launches_per_step(eulr_sim* sim);
 
-/* Runs ONE step with CUDA events between its launches on the simulation's
- * stream and returns the device time of each launch in milliseconds:
- * ms[0] ghost shell, ms[1] fused flux/update kernel, ms[2] dt finalize.
- * Synchronous; advances the state like eulr_sim_advance(sim, 1). */
+/* Runs ONE step with CUDA events around its launches on the simulation's
+ * stream and returns device times in milliseconds: ms[0] ghost layer (0
+ * except for the adjoint's recording steps), ms[1] the fused step kernel,
+ * ms[2] dt finalize (0 except on grids without interior cells, which launch
+ * no step kernel).  Synchronous; advances the state like
+ * eulr_sim_advance(sim, 1). */
 int eulr_sim_profile_step(eulr_sim* sim, float ms[3]);
 
 /* Conservation totals: sum over interior cells of (d, e, mx0, mx1, mx2),
@@ -293,9 +299,11 @@ int eulr_sim_state_bytes(eulr_sim* sim, long long* bytes_per_step);
 
 /* -------------------------------------------------------- multi-grid batch
  * Many independent grids of uneven sizes, each with its own gamma, mesh and
- * dt, advanced together: one persistent kernel launch per step pulls
+ * dt, advanced together: ONE persistent kernel launch per step pulls
  * (grid, tile, chunk) work items from a device work queue (largest grids
- * first), and pairs of steps replay from a CUDA graph.  The tile shape and
+ * first); each grid's last item to finish computes that grid's next dt and
+ * clock, and the launch's last CTA rewinds the queue.  Pairs of steps
+ * replay from a CUDA graph.  The tile shape and
  * chunk length are chosen by eulr_batch_autotune.  Loading functions work on
  * the batch's first state copy: load every grid before the first step (or
  * after an even number of steps). */

@@ -135,3 +135,62 @@ def test_fp32_batch_equals_single_grid_simulation(cuda, euler, precision):
             s.advance(9)
             ps, cs = s.state_numpy()
         assert np.array_equal(pb, ps) and np.array_equal(cb, cs)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32c"])
+def test_batch_with_grids_without_interior(cuda, euler, oracle_lib, precision):
+    """Grids with no interior cell have no work item: the step launch's last
+    CTA finalizes them (dt of their state, clock), as a finalize kernel did.
+    Their clock matches the oracle's loop on that grid; the other grids are
+    unaffected (FP64 against the oracle, FP32c against the FP64 batch)."""
+    grids, ics = draw_batch(17, ngrids=3)
+    grids.insert(1, (3, 3, 2, 1.3, 0.5, 0.5, 0.5))
+    ics.insert(1, (0.3, 0.5, 0.2))
+    grids.append((2, 5, 4, 1.5, 0.25, 0.2, 0.25))
+    ics.append((0.6, 0.3, 0.4))
+    steps = 7
+    with euler.Batch(grids, cfl=0.4, precision=precision) as b:
+        for g, (c, rr, pr) in enumerate(ics):
+            b.init_step(g, c, rr, pr)
+        b.advance(steps)
+        assert b.status() == 0
+        for g in range(len(grids)):
+            _, cref_state, tref = oracle_grid(oracle_lib, grids[g], ics[g], steps)
+            t, _, st = b.time(g)
+            assert st == steps
+            tol = 1e-12 if precision == "f64" else 1e-5
+            assert abs(t - tref) <= tol * tref, (g, t, tref)
+            if precision == "f64":
+                _, cons = b.state_numpy(g)
+                assert max(rel_linf(cons, cref_state)) <= 1e-11, g
+
+
+def test_batch_reload_after_even_steps(cuda, euler, oracle_lib):
+    """A grid loaded again after an even number of steps restarts from its new
+    state while the others run on: its ghost layer is set again (copy 1 at
+    load, copy 0 after its next step) and its clock starts from zero."""
+    grids, ics = draw_batch(23, ngrids=4)
+    with euler.Batch(grids, cfl=0.4) as b:
+        for g, (c, rr, pr) in enumerate(ics):
+            b.init_step(g, c, rr, pr)
+        b.advance(4)
+        c, rr, pr = ics[2]
+        b.init_step(2, c, rr, pr)
+        b.advance(6)
+        for g in range(len(grids)):
+            steps = 6 if g == 2 else 10
+            pref, cref, tref = oracle_grid(oracle_lib, grids[g], ics[g], steps)
+            t, _, st = b.time(g)
+            assert st == steps, g
+            assert abs(t - tref) <= 1e-12 * tref, g
+            prim, cons = b.state_numpy(g)
+            assert max(rel_linf(cons, cref) + rel_linf(prim, pref)) <= 1e-11, g
+
+
+def test_one_launch_per_step(cuda, euler):
+    n = 20
+    with euler.Simulation(n, n, n, precision="f64") as sim:
+        assert sim.launches_per_step() == 1
+        sim.init_implode()
+        ms = sim.profile_step()
+        assert ms[1] > 0.0
