@@ -198,6 +198,30 @@ __device__ __forceinline__ Prim7 get(float const* q, int idx)
     return v;
 }
 
+// ---- paired FP32 arithmetic: on sm_100 and later, FADD2/FMUL2/FFMA2
+// carry two FP32 operations per issued instruction, each rounded once.  The
+// step is bound by instruction issue, so the compensated update of fields
+// (d, e) and (m0, m1) runs in pairs (the same operations, the same bits).
+
+// a - b, rounded once (b * -1 is exact)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+
+// The compensated update of two fields of a cubic cell: u + k (flux balance)
+// with one rounding at the state's scale, operation for operation the scalar
+// form below.  nk = -k gives the product's rounding error negated,
+// P - k S, which the last step subtracts.
+__device__ __forceinline__ float2 comp_update2(float2 u, float2 xl, float2 xr, float2 yb, float2 yt, float2 zl, float2 zh,
+                                               float2 k, float2 nk)
+{
+    float2 const S = __fadd2_rn(__fadd2_rn(sub2(xl, xr), sub2(yb, yt)), sub2(zl, zh));
+    float2 const P = __fmul2_rn(k, S);
+    float2 const nP = __ffma2_rn(nk, S, P);
+    float2 const s = __fadd2_rn(u, P);
+    float2 const bb = sub2(s, u);
+    float2 const err = __fadd2_rn(sub2(u, sub2(s, bb)), sub2(P, bb));
+    return __fadd2_rn(s, sub2(err, nP));
+}
+
 struct ColShared {
     float slot[2][kFields * PLANE];
     float yflux[5][NT];
@@ -295,8 +319,21 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
         // ---- update of the own cell
         if (own) {
             float u[5] = {rk.d, rk.e, rk.m[0], rk.m[1], rk.m[2]};
+            constexpr bool kPaired = COMP == kCompSum && UNIFORM;
+            if (kPaired) { // fields (d, e) and (m0, m1) in pairs, m2 below
+                float2 const kk = make_float2(k0, k0), nk = make_float2(-k0, -k0);
 #pragma unroll
-            for (int f = 0; f < 5; ++f) {
+                for (int f = 0; f < 4; f += 2) {
+                    float2 const r = comp_update2(make_float2(u[f], u[f + 1]), make_float2(fxl[f], fxl[f + 1]),
+                                                  make_float2(fxr[f], fxr[f + 1]), make_float2(fyb[f], fyb[f + 1]),
+                                                  make_float2(fyt[f], fyt[f + 1]), make_float2(zlo[f], zlo[f + 1]),
+                                                  make_float2(fzh[f], fzh[f + 1]), kk, nk);
+                    u[f] = r.x;
+                    u[f + 1] = r.y;
+                }
+            }
+#pragma unroll
+            for (int f = kPaired ? 4 : 0; f < 5; ++f) {
                 if (COMP == kCompNone) {
                     u[f] = u[f] - k0 * (fxr[f] - fxl[f]) - k1 * (fyt[f] - fyb[f]) - k2 * (fzh[f] - zlo[f]);
                 } else if (UNIFORM) {
