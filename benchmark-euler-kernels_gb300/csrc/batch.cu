@@ -1,10 +1,11 @@
 // Multi-grid batch (eulr_batch_*): many independent grids of uneven sizes,
 // each with its own gamma, mesh and dt, advanced by ONE persistent kernel
 // launch per step that pulls (grid, tile, chunk) work items from a global
-// queue, largest grids first.  A step is three launches -- the ghost shells
-// of every grid (blockIdx.y = grid), the batch flux kernel, and a per-grid
-// dt finalize that also rewinds the queue -- and pairs of steps are captured
-// into a CUDA graph.  The tile shape (32x8, 16x8 or 16x16) and the chunk
+// queue, largest grids first.  That launch is the whole step: each grid's
+// last work item computes the grid's next dt and clock, and the launch's
+// last CTA rewinds the queue (and finalizes grids without interior cells).
+// Ghost layers are set at load (FP64: the first copy's once more after the
+// first step).  Pairs of steps are captured into a CUDA graph.  The tile shape (32x8, 16x8 or 16x16) and the chunk
 // length (planes per work item) are picked by eulr_batch_autotune, which
 // times every combination on the loaded state.
 //
