@@ -207,7 +207,8 @@ __device__ __forceinline__ float pressure_f32c(float d, float e, float m0, float
 // ------------------------------------------------------------------ HLLC
 // One side of a face in the face's frame: normal velocity un, tangential
 // velocities ut1/ut2 (in the cyclic order of the axes after the normal), sound
-// speed c and total energy density e.
+// speed c and, in `e`, the total energy density e (FP32) or e + p (FP64: the
+// FP64 HLLC needs only that sum, which the staging forms once per cell).
 template <class T>
 struct Side {
     T d, p, un, ut1, ut2, c, e;
@@ -294,7 +295,7 @@ __device__ __forceinline__ Flux<double> hllc_flux(Side<double> const& L, Side<do
     double const qun = left ? L.un : R.un;
     double const qut1 = left ? L.ut1 : R.ut1;
     double const qut2 = left ? L.ut2 : R.ut2;
-    double const qh = (left ? L.e : R.e) + qp; // e + p of the upwind side
+    double const qh = left ? L.e : R.e; // e + p of the upwind side
     double const qrc = left ? rc_L : rc_R;
 
     double const M = S * den - num; // den (S - ustar)

@@ -162,6 +162,9 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
             if (MODE == kModeStep) {
                 cs = __ldg(p.cs + o);
                 e = __ldg(p.cons_in.f[1] + o);
+                if constexpr (sizeof(T) == 8) {
+                    e += pr; // the FP64 HLLC takes e + p (once per staged cell, not per face)
+                }
             } else if (MODE == kModeStepCons) {
                 // cons-only FP32 state: cons_to_prim on chip
                 T const m0 = __ldg(p.cons_in.f[2] + o);
@@ -182,6 +185,9 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
                     cs = sqrt(p.gamma * pr * (T(1) / d));
                 }
                 e = pr * p.inv_gm1 + T(0.5) * d * (u0 * u0 + u1 * u1 + u2 * u2);
+                if constexpr (sizeof(T) == 8) {
+                    e += pr; // e + p, as the FP64 HLLC takes it
+                }
             }
         }
         q[0 * L::PLANE_PAD + c] = d;
@@ -466,6 +472,11 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
                 }
                 T const cs = fast_sound_speed((p.gamma * r) * pr);
                 if (MODE == kModeStep) {
+                    if constexpr (sizeof(T) == 8) {
+                        if (p.h_out != nullptr) {
+                            p.h_out[o] = u[1] + pr; // staged by TMA at the next step
+                        }
+                    }
                     p.prim_out.f[0][o] = u[0];
                     p.prim_out.f[1][o] = pr;
                     p.prim_out.f[2][o] = v0;
@@ -659,7 +670,7 @@ __global__ void __launch_bounds__(TX* TY) flux_batch_kernel(const __grid_constan
 {
     constexpr int NSLOT = 2;
     constexpr int NT = TX * TY;
-    static_assert(sizeof(FluxParams<T>) % 4 == 0 && sizeof(FluxParams<T>) / 4 <= NT, "parameter copy");
+    static_assert(sizeof(FluxParams<T>) % 4 == 0, "parameter copy in 4-byte words");
     extern __shared__ __align__(128) unsigned char smem_dyn[];
     __shared__ __align__(16) FluxParams<T> gp;
     __shared__ int s_item;
@@ -676,8 +687,8 @@ __global__ void __launch_bounds__(TX* TY) flux_batch_kernel(const __grid_constan
             break;
         }
         int4 const it = b.items[item];
-        if (tid < static_cast<int>(sizeof(FluxParams<T>) / 4)) {
-            reinterpret_cast<int*>(&gp)[tid] = reinterpret_cast<const int*>(&b.grids[it.x])[tid];
+        for (int w = tid; w < static_cast<int>(sizeof(FluxParams<T>) / 4); w += NT) {
+            reinterpret_cast<int*>(&gp)[w] = reinterpret_cast<const int*>(&b.grids[it.x])[w];
         }
         __syncthreads();
         T const dtodv = dt_over_dv(gp);
@@ -755,6 +766,9 @@ __device__ __forceinline__ void ghost_shell_body(GhostParams<T> const& p)
             for (int f = 0; f < 5; ++f) {
                 p.lo_out.f[f][o] = p.lo_in.f[f][o];
             }
+        }
+        if (p.h_out != nullptr) {
+            p.h_out[o] = e + pr;
         }
         if (p.prim_out.f[0] != nullptr) {
             p.prim_out.f[0][o] = d;

@@ -455,7 +455,7 @@ template <int COMP>
 __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant__ BatchParams<float> b)
 {
     static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
-    static_assert(sizeof(FluxParams<float>) % 4 == 0 && sizeof(FluxParams<float>) / 4 <= NT, "parameter copy");
+    static_assert(sizeof(FluxParams<float>) % 4 == 0, "parameter copy in 4-byte words");
     __shared__ __align__(16) ColShared sh;
     __shared__ __align__(16) FluxParams<float> gp;
     __shared__ int s_item;
@@ -473,8 +473,8 @@ __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant_
             break;
         }
         int4 const it = b.items[item];
-        if (tid < static_cast<int>(sizeof(FluxParams<float>) / 4)) {
-            reinterpret_cast<int*>(&gp)[tid] = reinterpret_cast<const int*>(&b.grids[it.x])[tid];
+        for (int w = tid; w < static_cast<int>(sizeof(FluxParams<float>) / 4); w += NT) {
+            reinterpret_cast<int*>(&gp)[w] = reinterpret_cast<const int*>(&b.grids[it.x])[w];
         }
         __syncthreads();
         float const dtodv = dt_over_dv(gp);

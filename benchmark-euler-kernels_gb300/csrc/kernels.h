@@ -64,6 +64,8 @@ struct FluxParams {
     int tiles_x, tiles_y, kchunk, nwork; // work decomposition (kchunk <= 0: default)
     int per_sm;                          // resident CTAs per SM (from configure_flux)
     SimScalars* fin;  // step mode, when set: the kernel finalizes the step itself (next dt, clock)
+    T* h_out;         // FP64 step mode, when set: e + p of the new state (interior), the HLLC's
+                      // energy-flux input, staged by TMA at the next step
     int grid_items;   // batch: work items of this grid in the current item list
 };
 
@@ -90,6 +92,7 @@ struct GhostParams {
     Bundle<T> prim_out;
     Bundle<T> prim_rec; // when set: a second copy of prim_out
     T* cs_out;
+    T* h_out;           // when set (FP64 state): e + p
     T gamma, gm1;
     T invdx0, invdx1, invdx2;
     unsigned long long* wmax;
@@ -108,7 +111,10 @@ cudaError_t launch_time_step(CBundle<T> prim, long long n, T gamma, T ix0, T ix1
 // first max wavespeed in one pass.
 template <class T>
 cudaError_t launch_load_prim(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma, T ix0, T ix1, T ix2,
-                             unsigned long long* wmax, int sms, cudaStream_t s);
+                             unsigned long long* wmax, int sms, cudaStream_t s, T* h = nullptr,
+                             const T* e_in = nullptr);
+// out = a + b elementwise, rounded once (the FP64 state's e + p after a restore).
+cudaError_t launch_add_fields(const double* a, const double* b, double* out, long long n, int sms, cudaStream_t s);
 cudaError_t launch_init_step(Bundle<double> prim, Geom g, double dx0, double dx1, double dx2, double c,
                              double rho_in, double p_in, double rho_out, double p_out, int sms, cudaStream_t s);
 // max invdt over all cells of a cons-only FP32 state (compensated: FP64

@@ -220,7 +220,8 @@ __global__ void __launch_bounds__(256) invdt_max_cons_kernel(CBundle<float> cons
 //    the max.
 template <class T>
 __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma,
-                                                        T gm1, T rgm1, T ix0, T ix1, T ix2, unsigned long long* wmax)
+                                                        T gm1, T rgm1, T ix0, T ix1, T ix2, unsigned long long* wmax,
+                                                        T* h, const T* e_in)
 {
     T local = T(0);
     WaveScreen screen(gamma, ix0, ix1, ix2);
@@ -241,11 +242,17 @@ __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<
             if (cons.f[0] != nullptr) {
                 T const int_e = div_by_rcp(p, gm1, rgm1);
                 T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
+                T const e = add_rn(ke, int_e);
                 cons.f[0][c] = d;
-                cons.f[1][c] = add_rn(ke, int_e);
+                cons.f[1][c] = e;
                 cons.f[2][c] = mul_rn(d, u0);
                 cons.f[3][c] = mul_rn(d, u1);
                 cons.f[4][c] = mul_rn(d, u2);
+                if (h != nullptr) {
+                    h[c] = add_rn(e, p);
+                }
+            } else if (h != nullptr) {
+                h[c] = add_rn(e_in[c], p);
             }
         }
         bool cand = valid;
@@ -349,11 +356,25 @@ cudaError_t launch_time_step(CBundle<T> prim, long long n, T gamma, T ix0, T ix1
 
 template <class T>
 cudaError_t launch_load_prim(CBundle<T> prim, Bundle<T> cons, T* cs, long long n, T gamma, T ix0, T ix1, T ix2,
-                             unsigned long long* wmax, int sms, cudaStream_t s)
+                             unsigned long long* wmax, int sms, cudaStream_t s, T* h, const T* e_in)
 {
     T const gm1 = gamma - T(1);
     load_prim_kernel<T><<<grid_for(n, sms), 256, 0, s>>>(prim, cons, cs, n, gamma, gm1, T(1) / gm1, ix0, ix1, ix2,
-                                                          wmax);
+                                                          wmax, h, e_in);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) add_fields_kernel(const double* a, const double* b, double* out, long long n)
+{
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        out[c] = __dadd_rn(a[c], b[c]);
+    }
+}
+
+cudaError_t launch_add_fields(const double* a, const double* b, double* out, long long n, int sms, cudaStream_t s)
+{
+    add_fields_kernel<<<grid_for(n, sms), 256, 0, s>>>(a, b, out, n);
     return cudaGetLastError();
 }
 
@@ -379,7 +400,7 @@ cudaError_t launch_invdt_max_cons(CBundle<float> cons, long long n, float gamma,
     template cudaError_t launch_time_step<T>(CBundle<T>, long long, T, T, T, T, T*, int, unsigned int*, T*,  \
                                              int, cudaStream_t);                                             \
     template cudaError_t launch_load_prim<T>(CBundle<T>, Bundle<T>, T*, long long, T, T, T, T, unsigned long long*,    \
-                                             int, cudaStream_t);
+                                             int, cudaStream_t, T*, const T*);
 
 EULR_INSTANTIATE_POINTWISE(double)
 EULR_INSTANTIATE_POINTWISE(float)

@@ -98,6 +98,7 @@ struct eulr_sim {
     void* cons[2][5] = {};
     void* lo[2][5] = {}; // compensated FP32 state with stored low words
     void* cs[2] = {};
+    void* h[2] = {};     // FP64: e + p, the HLLC's energy-flux input (staged by TMA instead of e)
     SimScalars* sc = nullptr;
     double* totals = nullptr;
     int cur = 0;
@@ -202,7 +203,7 @@ void setup_tma(eulr_sim* s)
     }
     for (int c = 0; c < 2; ++c) {
         void* f[7] = {s->prim[c][0], s->prim[c][1], s->prim[c][2], s->prim[c][3], s->prim[c][4], s->cs[c],
-                      s->cons[c][1]};
+                      s->h[c]};
         for (int i = 0; i < 7; ++i) {
             if (!encode_field_map(&s->maps[c].m[i], f[i], s->g)) {
                 return;
@@ -231,6 +232,7 @@ GhostParams<T> ghost_params(eulr_sim* s, int in, int out, unsigned long long* wm
     if (is_f64(s)) {
         gp.prim_out = bundle_of<T>(s->prim[out]);
         gp.cs_out = static_cast<T*>(s->cs[out]);
+        gp.h_out = static_cast<T*>(s->h[out]);
         if (s->rec[0] != nullptr) {
             gp.prim_rec = bundle_of<T>(reinterpret_cast<void* const*>(s->rec));
         }
@@ -278,6 +280,7 @@ int enqueue_step_t(eulr_sim* s, int in, cudaEvent_t* ev)
         p.cs = static_cast<const T*>(s->cs[in]);
         p.prim_out = bundle_of<T>(s->prim[out]);
         p.cs_out = static_cast<T*>(s->cs[out]);
+        p.h_out = static_cast<T*>(s->h[out]);
         if (s->rec[0] != nullptr) {
             p.prim_rec = bundle_of<T>(reinterpret_cast<void* const*>(s->rec));
         }
@@ -384,7 +387,9 @@ int prepare_loaded(eulr_sim* s, bool derive_cons = false)
             cv = bundle_of<double>(s->cons[0]);
         }
         SIM_CUDA(launch_load_prim<double>(pv, cv, static_cast<double*>(s->cs[0]), ncell(s), s->gamma, 1.0 / s->dx[0],
-                                          1.0 / s->dx[1], 1.0 / s->dx[2], &s->sc->wmax, s->sms, s->stream),
+                                          1.0 / s->dx[1], 1.0 / s->dx[2], &s->sc->wmax, s->sms, s->stream,
+                                          static_cast<double*>(s->h[0]),
+                                          derive_cons ? nullptr : static_cast<const double*>(s->cons[0][1])),
                  "load launch");
         SIM_CUDA(launch_finalize_dt<double>(s->sc, s->cfl, 0, s->stream), "finalize launch");
         SIM_TRY(set_ghost_layer(s)); // after the first dt, which the loaded ghost prim sets
@@ -543,6 +548,9 @@ int sim_restore(eulr_sim* s, const double* const* src, long long step)
     h.steps = step;
     SIM_CUDA(cudaMemcpyAsync(s->sc, &h, sizeof(h), cudaMemcpyHostToDevice, s->stream), "restore scalars");
     s->cur = 0;
+    SIM_CUDA(launch_add_fields(static_cast<const double*>(s->cons[0][1]), static_cast<const double*>(s->prim[0][1]),
+                               static_cast<double*>(s->h[0]), ncell(s), s->sms, s->stream),
+             "restore e + p");
     SIM_TRY(set_ghost_layer(s));
     SIM_CUDA(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize"); // h is a stack value
     s->host_steps = step;
@@ -619,8 +627,8 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
     size_t const field = pad256(static_cast<size_t>(ncell(s)) * s->esize);
     size_t const scal = pad256(sizeof(SimScalars));
     size_t const tot = pad256(kTotalsWork * sizeof(double));
-    // FP64: prim + cons + sound speed per copy; FP32: cons (+ low words) only
-    int const per_copy = is_f64(s) ? 11 : (s->comp == kCompHiLo ? 10 : 5);
+    // FP64: prim + cons + sound speed + e + p per copy; FP32: cons (+ low words) only
+    int const per_copy = is_f64(s) ? 12 : (s->comp == kCompHiLo ? 10 : 5);
     size_t const bytes = 2 * per_copy * field + scal + tot;
     e = cudaMalloc(&s->slab, bytes);
     if (e != cudaSuccess) {
@@ -634,6 +642,8 @@ int eulr_sim_create(int precision, int n0, int n1, int n2, double gamma, double 
                 b += field;
             }
             s->cs[c] = b;
+            b += field;
+            s->h[c] = b;
             b += field;
         }
         for (int f = 0; f < 5; ++f) {
