@@ -57,9 +57,9 @@ CFL = 0.4
 FLOPS_PER_CELL_DEFAULT = None
 
 # DRAM bytes (read + write) per interior cell of the fused FP64 kernel, from
-# one ncu capture at 192^3 (674 MB read + 580 MB written over 7.08 M interior
+# one ncu capture at 192^3 (736 MB read + 640 MB written over 7.08 M interior
 # cells); the kernel streams each plane once, so traffic scales with cells.
-FLUX_F64_DRAM_BYTES_PER_CELL = 177.3
+FLUX_F64_DRAM_BYTES_PER_CELL = 194.4
 
 
 def parse():
@@ -768,7 +768,7 @@ def run_ours(args):
             "kernel": "flux_tile_kernel<double, step>", "kernel_ms": flux_ms,
             "step_ms_sum_of_launches": step_ms_launches,
             "traffic": FLUX_F64_DRAM_BYTES_PER_CELL * interior,
-            "traffic_note": "dram bytes read+write per launch: 177.3 B per interior cell from an ncu capture at "
+            "traffic_note": "dram bytes read+write per launch: 194.4 B per interior cell from an ncu capture at "
                             "192^3, scaled by cells"}
     if fpc:
         fl = fpc["fused_step_fp64"] * interior
