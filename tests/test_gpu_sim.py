@@ -124,6 +124,11 @@ def test_set_state_and_odd_step_counts(cuda, euler, oracle_lib):
         pa, ca = a.state_numpy()
         pb, cb = b.state_numpy()
     assert np.array_equal(pa, pb) and np.array_equal(ca, cb)
+    # and both equal the oracle loop: a state loaded with its cons (the
+    # load reads e to form e + p) steps like one loaded from prim
+    p, c = prim0.copy(), cons0.copy()
+    O.simulate(p, c, 1.4, dx, 0.3, 7)
+    assert max(rel_linf(pa, p) + rel_linf(ca, c)) <= 1e-11
 
 
 def test_symmetry_of_implosion(cuda, euler):
