@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<
         bool cand = valid;
         if constexpr (sizeof(T) == 8) {
             if (valid) {
-                cs[c] = fast_sound_speed((gamma * rcp_faithful(d)) * p);
+                cs[c] = sqrt_quotient_faithful(gamma * p, d); // 1/rho is not needed here
             }
             cand = screen.exact_needed(valid, d, p, u0, u1, u2);
         } else if (valid) {

@@ -1,7 +1,9 @@
-// Accuracy check of the library's faithful FP64 reciprocal and square root
-// (rcp_faithful, sqrt_faithful in csrc/euler_device.cuh) against the
-// correctly rounded __drcp_rn / __dsqrt_rn, and of the PTX approximations
-// they refine.  Test harness, built and run by tests/test_gpu_faithful.py.
+// Accuracy check of the library's faithful FP64 reciprocal, square root and
+// square root of a quotient (rcp_faithful, sqrt_faithful,
+// sqrt_quotient_faithful in csrc/euler_device.cuh) against the correctly
+// rounded __drcp_rn / __dsqrt_rn / __dsqrt_rn(__ddiv_rn), and of the PTX
+// approximations they refine.  Test harness, built and run by
+// tests/test_gpu_faithful.py.
 //
 // Arguments m * 2^e with m uniform in [1, 2) and e uniform in [-100, 100]
 // (4M of them, a fixed LCG stream), plus the binade edges 1, 2 - ulp, 2^e.
@@ -23,6 +25,9 @@ __global__ void check_kernel(const double* x, double* out, int n)
         return;
     }
     double const v = x[i];
+    double const w = x[(static_cast<long long>(i) * 7 + 3) % n]; // a second argument for the quotient
+    out[6 * static_cast<long long>(n) + 2 * static_cast<long long>(i) + 0] = __dsqrt_rn(__ddiv_rn(v, w));
+    out[6 * static_cast<long long>(n) + 2 * static_cast<long long>(i) + 1] = eulr::sqrt_quotient_faithful(v, w);
     double ra, sa;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(ra) : "d"(v));
     asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(sa) : "d"(v));
@@ -66,7 +71,7 @@ int main()
     double* dx = nullptr;
     double* dout = nullptr;
     if (cudaMalloc(&dx, sizeof(double) * n) != cudaSuccess ||
-        cudaMalloc(&dout, sizeof(double) * 6 * static_cast<size_t>(n)) != cudaSuccess) {
+        cudaMalloc(&dout, sizeof(double) * 8 * static_cast<size_t>(n)) != cudaSuccess) {
         std::printf("cudaMalloc failed\n");
         return 1;
     }
@@ -77,12 +82,12 @@ int main()
         std::printf("kernel failed: %s\n", cudaGetErrorString(err));
         return 1;
     }
-    std::vector<double> o(6 * static_cast<size_t>(n));
+    std::vector<double> o(8 * static_cast<size_t>(n));
     cudaMemcpy(o.data(), dout, sizeof(double) * o.size(), cudaMemcpyDeviceToHost);
     cudaFree(dx);
     cudaFree(dout);
     double rcp_approx = 0.0, rsqrt_approx = 0.0;
-    long long rcp_ulp = 0, sqrt_ulp = 0, rcp_diff = 0, sqrt_diff = 0;
+    long long rcp_ulp = 0, sqrt_ulp = 0, rcp_diff = 0, sqrt_diff = 0, quot_ulp = 0;
     for (int i = 0; i < n; ++i) {
         double const* r = o.data() + 6 * static_cast<size_t>(i);
         rcp_approx = std::fmax(rcp_approx, std::fabs(r[0] * h[static_cast<size_t>(i)] - 1.0));
@@ -93,9 +98,12 @@ int main()
         sqrt_ulp = ds > sqrt_ulp ? ds : sqrt_ulp;
         rcp_diff += du != 0;
         sqrt_diff += ds != 0;
+        double const* qv = o.data() + 6 * static_cast<size_t>(n) + 2 * static_cast<size_t>(i);
+        long long const dq = std::llabs(bits(qv[1]) - bits(qv[0]));
+        quot_ulp = dq > quot_ulp ? dq : quot_ulp;
     }
     std::printf("{\"n\": %d, \"rcp_approx_rel\": %.6e, \"rsqrt_approx_rel\": %.6e, \"rcp_max_ulp\": %lld, "
-                "\"sqrt_max_ulp\": %lld, \"rcp_differ\": %lld, \"sqrt_differ\": %lld}\n",
-                n, rcp_approx, rsqrt_approx, rcp_ulp, sqrt_ulp, rcp_diff, sqrt_diff);
+                "\"sqrt_max_ulp\": %lld, \"rcp_differ\": %lld, \"sqrt_differ\": %lld, \"quot_max_ulp\": %lld}\n",
+                n, rcp_approx, rsqrt_approx, rcp_ulp, sqrt_ulp, rcp_diff, sqrt_diff, quot_ulp);
     return 0;
 }
