@@ -86,14 +86,20 @@ __device__ __forceinline__ void prep_cell(AdjParams const& p, CBundle<double> co
     double const u0 = prim.f[2][c];
     double const u1 = prim.f[3][c];
     double const u2 = prim.f[4][c];
-    double const R = rcp_faithful(d * pr);
-    double const inv_d = pr * R;
-    double const inv_p = d * R;
-    double const c2 = (p.gamma * pr) * inv_d;
-    double const cs = sqrt_faithful(c2);
+    // with y = 1/sqrt(gamma p rho) (one faithful reciprocal square root):
+    // c = gamma p y, dc/dp = c/(2p) = gamma y / 2, 1/rho = gamma p y^2 and
+    // dc/drho = -c/(2 rho)
+    double const gp = p.gamma * pr;
+    double const z = gp * d;
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(z));
+    double const e = __fma_rn(-(z * y), y, 1.0);
+    y = __fma_rn(y, e * __fma_rn(0.375, e, 0.5), y); // third-order step, as sqrt_faithful's
+    double const cs = gp * y;
+    double const inv_d = cs * y;
     double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
     p.w.derived[0][c] = cs;
-    p.w.derived[1][c] = 0.5 * cs * inv_p;
+    p.w.derived[1][c] = (0.5 * p.gamma) * y;
     p.w.derived[2][c] = -0.5 * cs * inv_d;
     p.w.derived[3][c] = pr * p.inv_gm1 + d * ke;
     p.w.derived[4][c] = ke;
