@@ -232,6 +232,11 @@ struct full_extent_t
     explicit full_extent_t() = default;
 };
 inline constexpr full_extent_t full_extent {};
+// Kokkos's own spellings of these slices
+inline constexpr full_extent_t ALL {};
+template <class A, class B>
+using pair = std::pair<A, B>;
+using std::make_pair;
 
 namespace detail {
 enum class slice_kind { index, full, range };

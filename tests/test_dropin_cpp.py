@@ -157,7 +157,7 @@ int main() {
     dump("e_p", e.p);
     auto g = subspan(p, 6, 4, 3);
     dump("g_d", g.d);
-    auto h = subspan(p, all, std::pair<int, int>(1, 4), all);
+    auto h = subspan(p, Kokkos::ALL, Kokkos::make_pair(1, 4), Kokkos::full_extent);
     static_assert(std::is_same_v<decltype(h.d)::layout_type, Kokkos::layout_stride>);
     dump("h_d", h.d);
     // a contiguous slab is still an operator argument
