@@ -114,6 +114,24 @@ __device__ __forceinline__ double sqrt_faithful(double x)
     return __fma_rn(t, e * q, t);
 }
 
+// The hardware's FP32 approximations themselves (one MUFU instruction each,
+// relative error below 2^-22): the FP32 steps' error is set by the state's
+// own rounding.  Inputs are normal positive numbers there; ftz maps a
+// subnormal input to zero (1/x = +inf) and a result below 2^-126 to zero,
+// which no physical state reaches.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // sqrt(x / d) for x, d > 0 without a reciprocal: x * rsqrt(x d), the PTX
 // approximation of 1/sqrt refined by the third-order step of sqrt_faithful
 // (y (1 + e/2 + 3e^2/8), e = 1 - z y^2).  Seven FP64 instructions and one
@@ -224,8 +242,8 @@ __device__ __forceinline__ float pressure_f32c(float d, float e, float m0, float
 // ------------------------------------------------------------------ HLLC
 // One side of a face in the face's frame: normal velocity un, tangential
 // velocities ut1/ut2 (in the cyclic order of the axes after the normal), sound
-// speed c and, in `e`, the total energy density e (FP32) or e + p (FP64: the
-// FP64 HLLC needs only that sum, which the staging forms once per cell).
+// speed c and, in `e`, the sum e + p of total energy density and pressure:
+// the HLLC needs only that sum, which the staging forms once per cell.
 template <class T>
 struct Side {
     T d, p, un, ut1, ut2, c, e;
@@ -341,7 +359,8 @@ __device__ __forceinline__ Flux<double> hllc_flux(Side<double> const& L, Side<do
     return f;
 }
 
-// FP32 version (real_t = float operators): same algebra, FP32 min/max.
+// FP32 version (real_t = float operators): same algebra, FP32 min/max and
+// the hardware reciprocal.
 __device__ __forceinline__ Flux<float> hllc_flux(Side<float> const& L, Side<float> const& R)
 {
     float const cmax = fmaxf(L.c, R.c);
@@ -360,11 +379,10 @@ __device__ __forceinline__ Flux<float> hllc_flux(Side<float> const& L, Side<floa
     float const qun = left ? L.un : R.un;
     float const qut1 = left ? L.ut1 : R.ut1;
     float const qut2 = left ? L.ut2 : R.ut2;
-    float const qe = left ? L.e : R.e;
+    float const qh = left ? L.e : R.e; // e + p of the upwind side
     float const qrc = left ? rc_L : rc_R;
     float const M = S * den - num;
-    float const Rr = __fdividef(1.0f, den * M); // hardware reciprocal (<= 2 ulp): |den M| is far from the
-                                                 // ends of the float range for any physical state
+    float const Rr = rcp_approx(den * M); // |den M| is far from the ends of the float range for any physical state
     float const ustar = num * (M * Rr);
     float const inv = den * (den * Rr);
     float const w = ustar - qun;
@@ -372,14 +390,14 @@ __device__ __forceinline__ Flux<float> hllc_flux(Side<float> const& L, Side<floa
     bool const supersonic = S_L * S_R > 0.0f;
     float const ratio = (S - qun) * inv;
     float const d_star = ratio * qd;
-    float const e_star = ratio * qe + w * (qp + qrc * ustar) * inv;
+    float const h_star = ratio * qh + w * (S * d_star); // e_star + pstar
     float const un_o = supersonic ? qun : ustar;
     float const ptot_o = supersonic ? qp : pstar;
     float const d_o = supersonic ? qd : d_star;
-    float const e_o = supersonic ? qe : e_star;
+    float const h_o = supersonic ? qh : h_star;
     Flux<float> f;
     f.d = d_o * un_o;
-    f.e = (e_o + ptot_o) * un_o;
+    f.e = h_o * un_o;
     f.n = f.d * un_o + ptot_o;
     f.t1 = f.d * qut1;
     f.t2 = f.d * qut2;

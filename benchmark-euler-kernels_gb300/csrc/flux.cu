@@ -162,9 +162,6 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
             if (MODE == kModeStep) {
                 cs = __ldg(p.cs + o);
                 e = __ldg(p.cons_in.f[1] + o);
-                if constexpr (sizeof(T) == 8) {
-                    e += pr; // the FP64 HLLC takes e + p (once per staged cell, not per face)
-                }
             } else if (MODE == kModeStepCons) {
                 // cons-only FP32 state: cons_to_prim on chip
                 T const m0 = __ldg(p.cons_in.f[2] + o);
@@ -185,10 +182,8 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
                     cs = sqrt(p.gamma * pr * (T(1) / d));
                 }
                 e = pr * p.inv_gm1 + T(0.5) * d * (u0 * u0 + u1 * u1 + u2 * u2);
-                if constexpr (sizeof(T) == 8) {
-                    e += pr; // e + p, as the FP64 HLLC takes it
-                }
             }
+            e += pr; // the HLLC takes e + p (formed once per staged cell, not per face)
         }
         q[0 * L::PLANE_PAD + c] = d;
         q[1 * L::PLANE_PAD + c] = pr;

@@ -15,15 +15,20 @@ namespace {
 // (i0 + ti, j0 + tj) and marches it up z, keeping its cell's primitive state
 // of planes k and k+1 in registers.  Per plane it solves
 //   x: the face on its cell's left  (the right one is lane+1's, by shuffle;
-//      lane 31 also solves the tile's right boundary face),
+//      the tile's 8 right boundary faces are solved by the first 8 lanes of
+//      one warp and read by lane 31 from shared memory: solved in lane 31 of
+//      every warp, each would cost its warp a whole extra HLLC of issue),
 //   y: the face below its cell      (the one above is the next row's, through
 //      shared memory; row 7 also solves the tile's top boundary faces),
 //   z: the face above its cell      (both sides in registers; the face below
 //      is the previous plane's).
-// Shared memory holds only plane k's primitive tile with its halo ring (for
-// the y and boundary neighbours) and the y fluxes.  Cons of plane k+2 (own
-// cell) and k+1 (halo ring, threads 0..79) are prefetched into registers a
-// plane ahead.
+// Shared memory holds two slots of primitive tiles with their halo rings
+// (for the y and boundary neighbours): plane k's, read by the faces, and
+// plane k+1's, whose halo ring (threads 0..79) is staged meanwhile, so that
+// no halo conversion stands between a plane's own staging and its barrier.
+// The y fluxes and the right boundary fluxes go through shared memory too.
+// Cons of plane k+2 (own cell) and k+2 (halo ring) are prefetched with
+// cp.async a plane before they are converted.
 //
 // Plain (kCompNone) and compensated (kCompSum) FP32 states; the state with
 // stored low words (kCompHiLo) keeps the shared-memory tile engine, whose
@@ -55,9 +60,15 @@ constexpr int HX = TX + 2;
 constexpr int HY = TY + 2;
 constexpr int PLANE = HX * HY; // 340
 constexpr int NHALO = 2 * TY + 2 * TX; // 80: left, right columns, bottom, top rows
+// The warp whose first TY lanes solve the tile's right boundary x faces: one
+// without halo staging (threads 0..NHALO-1) and other than the top row's warp
+// (which solves the top boundary y faces), so that no warp solves more than
+// one extra face per plane.
+constexpr int kRightWarp = 3;
+static_assert(kRightWarp * 32 >= NHALO && kRightWarp < TY - 1 && TY <= 32, "right boundary warp");
 
 struct Prim7 {
-    float d, p, u[3], c, e;
+    float d, p, u[3], c, e; // e: e + p, as the HLLC takes it
 };
 
 struct Raw5 {
@@ -87,22 +98,22 @@ __device__ __forceinline__ void to_global(Flux<float> const& f, int dir, float* 
     g[2 + (dir + 2) % 3] = f.t2;
 }
 
-// Primitive state, sound speed and energy of an FP32 conservative cell.  1/rho
-// is the hardware reciprocal (MUFU.RCP, within 1 ulp), not the correctly
-// rounded sequence: the FP32 step's error budget is set by the state's own
-// rounding, and the 1000-step implosion error is the same either way.
+// Primitive state, sound speed and e + p of an FP32 conservative cell.  1/rho
+// is the hardware reciprocal (one MUFU.RCP), not the correctly rounded
+// sequence: the FP32 step's error budget is set by the state's own rounding,
+// and the 1000-step implosion error is the same either way.
 template <int COMP>
 __device__ __forceinline__ Prim7 prim_of(Raw5 const& r, FluxParams<float> const& p)
 {
     Prim7 q;
-    float const ir = __fdividef(1.0f, r.d);
+    float const ir = rcp_approx(r.d);
     q.d = r.d;
-    q.e = r.e;
     q.u[0] = r.m[0] * ir;
     q.u[1] = r.m[1] * ir;
     q.u[2] = r.m[2] * ir;
     q.p = cons_pressure<COMP>(r.d, r.e, r.m[0], r.m[1], r.m[2], ir, p.gm1, nullptr);
     q.c = fast_sound_speed(p.gamma * q.p * ir);
+    q.e = __fadd_rn(r.e, q.p);
     return q;
 }
 
@@ -132,6 +143,9 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src)
 }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// All of this thread's copy groups but the last committed one have landed.
+__device__ __forceinline__ void cp_async_wait_all_but_last() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Starts copying the cons of cell (i, j, k) to dst[f * stride] (benign values for cells outside the array).
 __device__ __forceinline__ void prefetch_raw(float* dst, int stride, FluxParams<float> const& p, int i, int j, int k)
@@ -225,6 +239,7 @@ __device__ __forceinline__ float2 comp_update2(float2 u, float2 xl, float2 xr, f
 struct ColShared {
     float slot[2][kFields * PLANE];
     float yflux[5][NT];
+    float xflux_r[5][TY]; // the tile's right boundary x faces
     float raw_own[5 * NT];     // own column, two planes ahead
     float raw_halo[5 * NHALO]; // halo ring, one plane ahead
     long long warp_best[NT / 32];
@@ -254,11 +269,17 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
     int const j = j0 + tj;
     bool const own = (i < p.g.n0 - 1) && (j < p.g.n1 - 1);
 
-    // prologue: planes kb-1 (z face below), kb, kb+1 of the own column,
-    // plane kb of the halo ring
+    // prologue: plane kb of the halo ring staged, kb+1 on its way; planes
+    // kb-1 (z face below), kb, kb+1 of the own column
     if (tid < NHALO) {
         prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
+        cp_async_wait_all();
+        put(sh.slot[0], hhy * HX + hhx, prim_of<COMP>(read_raw(sh.raw_halo + tid, NHALO), p));
+        if (kb + 1 < ke) {
+            prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb + 1);
+        }
     }
+    cp_async_commit();
     Raw5 const rb = load_raw(p, i, j, kb - 1);
     Raw5 rk = load_raw(p, i, j, kb);
     Raw5 rn = load_raw(p, i, j, kb + 1); // kb + 1 <= ke <= n2 - 1
@@ -268,22 +289,31 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
     to_global(hllc_flux(side_of(prim_of<COMP>(rb, p), 2), side_of(q0, 2)), 2, zlo);
     long long o = p.g.at(min(i, p.g.n0 - 1), min(j, p.g.n1 - 1), kb);
 
+    // Unrolled twice on the compensated state: the plane-to-plane register
+    // rotation (q0 <- q1, rk <- rn, zlo <- fzh) becomes renaming instead of
+    // moves, and the slot of each copy is a constant.
+#pragma unroll(COMP == kCompSum ? 2 : 1)
     for (int k = kb; k < ke; ++k) {
         float* const q = sh.slot[(k - kb) & 1];
-        // stage plane k: the own cell and the halo ring
+        // stage plane k: the own cell (its halo ring was staged a plane ahead)
         put(q, own_idx, q0);
-        if (tid < NHALO) {
-            cp_async_wait_all(); // this thread's copies of the halo cell (plane k) landed
-            put(q, hhy * HX + hhx, prim_of<COMP>(read_raw(sh.raw_halo + tid, NHALO), p));
-            if (k + 1 < ke) {
-                prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 1);
-            }
-        }
         // own column plane k+2, consumed at the end of this plane
         if (k + 2 <= ke) {
             prefetch_raw(sh.raw_own + tid, NT, p, i, j, k + 2);
         }
+        cp_async_commit();
         __syncthreads(); // plane k staged
+        // the halo ring of plane k+1 into the other slot, off the path to the
+        // barrier above (the slot's last reader finished before the previous
+        // plane's second barrier)
+        if (tid < NHALO && k + 1 < ke) {
+            cp_async_wait_all_but_last(); // the halo copies of plane k+1 landed (own k+2 may be in flight)
+            put(sh.slot[(k + 1 - kb) & 1], hhy * HX + hhx, prim_of<COMP>(read_raw(sh.raw_halo + tid, NHALO), p));
+            if (k + 2 < ke) {
+                prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 2);
+            }
+        }
+        cp_async_commit();
 
         // ---- faces
         float fxl[5], fyb[5], fzh[5], fxr[5], fyt[5];
@@ -301,19 +331,27 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
         for (int f = 0; f < 5; ++f) {
             fxr[f] = __shfl_down_sync(0xffffffffu, fxl[f], 1);
         }
-        if (ti == TX - 1) { // the tile's right boundary face
-            to_global(hllc_flux(side_of(q0, 0), side_of(get(q, own_idx + 1), 0)), 0, fxr);
+        if (tj == kRightWarp && ti < TY) { // the tile's right boundary faces, one per row
+            int const c = (ti + 1) * HX + TX;
+            float t[5];
+            to_global(hllc_flux(side_of(get(q, c), 0), side_of(get(q, c + 1), 0)), 0, t);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                sh.xflux_r[f][ti] = t[f];
+            }
         }
         if (tj == TY - 1) { // the tile's top boundary faces
             to_global(hllc_flux(side_of(q0, 1), side_of(get(q, own_idx + HX), 1)), 1, fyt);
         }
-        __syncthreads(); // y fluxes written
+        __syncthreads(); // y fluxes and right boundary fluxes written
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
             fyb[f] = sh.yflux[f][tid];
             if (tj < TY - 1) {
                 fyt[f] = sh.yflux[f][tid + TX];
             }
+            float const xr = sh.xflux_r[f][tj]; // one broadcast read per warp
+            fxr[f] = ti == TX - 1 ? xr : fxr[f];
         }
 
         // ---- update of the own cell
@@ -365,7 +403,7 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
                 p.cons_out.f[f][o] = u[f];
             }
             // next step's CFL wavespeed of the new state (time_step.hpp:28-33)
-            float const r = __fdividef(1.0f, u[0]);
+            float const r = rcp_approx(u[0]);
             float const v0 = u[2] * r, v1 = u[3] * r, v2 = u[4] * r;
             float const pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1, nullptr);
             float const cs = fast_sound_speed((p.gamma * r) * pr);
@@ -382,7 +420,7 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
         rk = rn;
         q0 = q1;
         if (k + 2 <= ke) {
-            cp_async_wait_all();
+            cp_async_wait_all_but_last(); // the own copies of plane k+2 landed
             rn = read_raw(sh.raw_own + tid, NT);
             q1 = prim_of<COMP>(rn, p);
         }

@@ -38,7 +38,7 @@ __device__ __forceinline__ double cons_pressure(double, double, double, double, 
 // Sound speed sqrt(gamma p / rho), faithful: fewer FP64 instructions than a
 // correctly rounded sqrt, within one ulp of it.
 __device__ __forceinline__ double fast_sound_speed(double c2) { return sqrt_faithful(c2); }
-__device__ __forceinline__ float fast_sound_speed(float c2) { return c2 * rsqrtf(c2); }
+__device__ __forceinline__ float fast_sound_speed(float c2) { return c2 * rsqrt_approx(c2); }
 
 __device__ __forceinline__ long long wave_key(double v)
 {
