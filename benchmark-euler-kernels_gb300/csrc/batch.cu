@@ -286,6 +286,9 @@ int enqueue_step_t(eulr_batch* b, int dir)
     bp.exited = b->d_exited;
     bp.idle = b->d_idle;
     bp.nidle = b->nidle;
+    for (auto const& gs : b->grids) {
+        bp.max_cells = std::max(bp.max_cells, gs.g.ncell());
+    }
     long long grid = static_cast<long long>(b->sms) * b->per_sm;
     if (grid > b->nitems) {
         grid = b->nitems > 0 ? b->nitems : 1;

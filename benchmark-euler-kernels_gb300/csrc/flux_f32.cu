@@ -120,12 +120,23 @@ __device__ __forceinline__ Prim7 prim_of(Raw5 const& r, FluxParams<float> const&
 // A benign state for cells outside the array (no face touching one is used).
 __device__ __forceinline__ Raw5 outside() { return Raw5{1.0f, 2.5f, {0.0f, 0.0f, 0.0f}}; }
 
+// Element offset of cell (i, j, k) in the type Off: unsigned (32-bit
+// arithmetic, one instruction fewer per address) when the grid has fewer
+// than 2^32 cells, long long otherwise.
+template <class Off>
+__device__ __forceinline__ Off cell_offset(Geom const& g, int i, int j, int k)
+{
+    return static_cast<Off>(i) + static_cast<Off>(g.s1) * static_cast<Off>(j) +
+           static_cast<Off>(g.s2) * static_cast<Off>(k);
+}
+
+template <class Off>
 __device__ __forceinline__ Raw5 load_raw(FluxParams<float> const& p, int i, int j, int k)
 {
     if (i >= p.g.n0 || j >= p.g.n1) {
         return outside();
     }
-    long long const o = p.g.at(i, j, k);
+    Off const o = cell_offset<Off>(p.g, i, j, k);
     Raw5 r;
     r.d = __ldg(p.cons_in.f[0] + o);
     r.e = __ldg(p.cons_in.f[1] + o);
@@ -148,6 +159,7 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all_but_last() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Starts copying the cons of cell (i, j, k) to dst[f * stride] (benign values for cells outside the array).
+template <class Off>
 __device__ __forceinline__ void prefetch_raw(float* dst, int stride, FluxParams<float> const& p, int i, int j, int k)
 {
     if (i >= p.g.n0 || j >= p.g.n1) {
@@ -159,7 +171,7 @@ __device__ __forceinline__ void prefetch_raw(float* dst, int stride, FluxParams<
         dst[4 * stride] = b.m[2];
         return;
     }
-    long long const o = p.g.at(i, j, k);
+    Off const o = cell_offset<Off>(p.g, i, j, k);
 #pragma unroll
     for (int f = 0; f < 5; ++f) {
         cp_async4(dst + f * stride, p.cons_in.f[f] + o);
@@ -249,7 +261,7 @@ struct ColShared {
 // One work item: interior planes [kb, ke) of the 32 x 8 column tile (tx, ty),
 // kb = 1 + kc * kchunk, with update coefficients k0..k2 (all equal when UNIFORM).
 // Accumulates this thread's max wavespeed and non-physical flag.
-template <int COMP, bool UNIFORM>
+template <int COMP, bool UNIFORM, class Off>
 __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, float k1, float k2, int tx, int ty,
                                          int kc, ColShared& sh, float& wmaxf, bool& bad)
 {
@@ -272,34 +284,34 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
     // prologue: plane kb of the halo ring staged, kb+1 on its way; planes
     // kb-1 (z face below), kb, kb+1 of the own column
     if (tid < NHALO) {
-        prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
+        prefetch_raw<Off>(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb);
         cp_async_wait_all();
         put(sh.slot[0], hhy * HX + hhx, prim_of<COMP>(read_raw(sh.raw_halo + tid, NHALO), p));
         if (kb + 1 < ke) {
-            prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb + 1);
+            prefetch_raw<Off>(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, kb + 1);
         }
     }
     cp_async_commit();
-    Raw5 const rb = load_raw(p, i, j, kb - 1);
-    Raw5 rk = load_raw(p, i, j, kb);
-    Raw5 rn = load_raw(p, i, j, kb + 1); // kb + 1 <= ke <= n2 - 1
+    Raw5 const rb = load_raw<Off>(p, i, j, kb - 1);
+    Raw5 rk = load_raw<Off>(p, i, j, kb);
+    Raw5 rn = load_raw<Off>(p, i, j, kb + 1); // kb + 1 <= ke <= n2 - 1
     Prim7 q0 = prim_of<COMP>(rk, p);
     Prim7 q1 = prim_of<COMP>(rn, p);
     float zlo[5];
     to_global(hllc_flux(side_of(prim_of<COMP>(rb, p), 2), side_of(q0, 2)), 2, zlo);
-    long long o = p.g.at(min(i, p.g.n0 - 1), min(j, p.g.n1 - 1), kb);
+    Off o = cell_offset<Off>(p.g, min(i, p.g.n0 - 1), min(j, p.g.n1 - 1), kb);
 
-    // Unrolled twice on the compensated state: the plane-to-plane register
-    // rotation (q0 <- q1, rk <- rn, zlo <- fzh) becomes renaming instead of
-    // moves, and the slot of each copy is a constant.
-#pragma unroll(COMP == kCompSum ? 2 : 1)
+    // Unrolled twice: the plane-to-plane register rotation (q0 <- q1,
+    // rk <- rn, zlo <- fzh) becomes renaming instead of moves, and the slot
+    // of each copy is a constant.
+#pragma unroll 2
     for (int k = kb; k < ke; ++k) {
         float* const q = sh.slot[(k - kb) & 1];
         // stage plane k: the own cell (its halo ring was staged a plane ahead)
         put(q, own_idx, q0);
         // own column plane k+2, consumed at the end of this plane
         if (k + 2 <= ke) {
-            prefetch_raw(sh.raw_own + tid, NT, p, i, j, k + 2);
+            prefetch_raw<Off>(sh.raw_own + tid, NT, p, i, j, k + 2);
         }
         cp_async_commit();
         __syncthreads(); // plane k staged
@@ -310,7 +322,7 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
             cp_async_wait_all_but_last(); // the halo copies of plane k+1 landed (own k+2 may be in flight)
             put(sh.slot[(k + 1 - kb) & 1], hhy * HX + hhx, prim_of<COMP>(read_raw(sh.raw_halo + tid, NHALO), p));
             if (k + 2 < ke) {
-                prefetch_raw(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 2);
+                prefetch_raw<Off>(sh.raw_halo + tid, NHALO, p, i0 - 1 + hhx, j0 - 1 + hhy, k + 2);
             }
         }
         cp_async_commit();
@@ -424,7 +436,7 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
             rn = read_raw(sh.raw_own + tid, NT);
             q1 = prim_of<COMP>(rn, p);
         }
-        o += p.g.s2;
+        o += static_cast<Off>(p.g.s2);
     }
     __syncthreads(); // the slots are restaged by the next item
 }
@@ -468,7 +480,7 @@ __device__ __forceinline__ void col_flush(ColShared& sh, float& wmaxf, bool& bad
     bad = false;
 }
 
-template <int COMP, bool UNIFORM>
+template <int COMP, bool UNIFORM, class Off>
 __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__ FluxParams<float> p)
 {
     static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
@@ -479,7 +491,7 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
     bool bad = false;
     int const tiles_xy = p.tiles_x * p.tiles_y;
     for (int w = blockIdx.x; w < p.nwork; w += gridDim.x) {
-        col_item<COMP, UNIFORM>(p, k0, k1, k2, w % p.tiles_x, (w / p.tiles_x) % p.tiles_y, w / tiles_xy, sh, wmaxf,
+        col_item<COMP, UNIFORM, Off>(p, k0, k1, k2, w % p.tiles_x, (w / p.tiles_x) % p.tiles_y, w / tiles_xy, sh, wmaxf,
                                 bad);
     }
     col_flush(sh, wmaxf, bad, p.wmax, p.status);
@@ -489,7 +501,7 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
 // The column engine over a batch: CTAs pop (grid, tile x, tile y, chunk)
 // items from the queue, as flux_batch_kernel does; each item's wavespeed goes
 // to its own grid.  Grids with equal face areas take the cubic update.
-template <int COMP>
+template <int COMP, class Off>
 __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant__ BatchParams<float> b)
 {
     static_assert(COMP == kCompNone || COMP == kCompSum, "low-word states use the tile engine");
@@ -518,9 +530,9 @@ __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant_
         float const dtodv = dt_over_dv(gp);
         float const k0 = dtodv * gp.ds0, k1 = dtodv * gp.ds1, k2 = dtodv * gp.ds2;
         if (gp.ds0 == gp.ds1 && gp.ds1 == gp.ds2) {
-            col_item<COMP, true>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
+            col_item<COMP, true, Off>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
         } else {
-            col_item<COMP, false>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
+            col_item<COMP, false, Off>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
         }
         col_flush(sh, wmaxf, bad, gp.wmax, gp.status);
         item_done(gp);
@@ -530,11 +542,14 @@ __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant_
 
 } // namespace f32col
 
+// Grids up to this many cells index their fields with 32-bit offsets.
+constexpr long long kNarrowCells = 0xffffffffLL;
+
 template <int COMP>
 cudaError_t configure_f32col(int* per_sm)
 {
     int n = 0;
-    cudaError_t const e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_step_kernel<COMP, false>,
+    cudaError_t const e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_step_kernel<COMP, false, long long>,
                                                                         f32col::NT, 0);
     *per_sm = n < 1 ? 1 : n;
     return e;
@@ -561,10 +576,17 @@ cudaError_t launch_f32col(FluxParams<float> p, int sms, cudaStream_t s)
     p.nwork = static_cast<int>(nwork);
     long long const grid = slots < nwork ? slots : nwork;
     // equal face areas (cubic cells) give equal update coefficients dt/dv * ds_d
-    if (p.ds0 == p.ds1 && p.ds1 == p.ds2) {
-        f32col::f32_step_kernel<COMP, true><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
+    bool const uniform = p.ds0 == p.ds1 && p.ds1 == p.ds2;
+    if (p.g.ncell() <= kNarrowCells) {
+        if (uniform) {
+            f32col::f32_step_kernel<COMP, true, unsigned><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
+        } else {
+            f32col::f32_step_kernel<COMP, false, unsigned><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
+        }
+    } else if (uniform) {
+        f32col::f32_step_kernel<COMP, true, long long><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
     } else {
-        f32col::f32_step_kernel<COMP, false><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
+        f32col::f32_step_kernel<COMP, false, long long><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);
     }
     return cudaGetLastError();
 }
@@ -576,13 +598,17 @@ struct ColBatchKernel {
     {
         int n = 0;
         cudaError_t const e =
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_batch_kernel<COMP>, f32col::NT, 0);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f32col::f32_batch_kernel<COMP, long long>, f32col::NT, 0);
         *per_sm = n < 1 ? 1 : n;
         return e;
     }
     static cudaError_t launch(BatchParams<float> const& b, int grid, cudaStream_t s)
     {
-        f32col::f32_batch_kernel<COMP><<<grid, f32col::NT, 0, s>>>(b);
+        if (b.max_cells <= kNarrowCells) {
+            f32col::f32_batch_kernel<COMP, unsigned><<<grid, f32col::NT, 0, s>>>(b);
+        } else {
+            f32col::f32_batch_kernel<COMP, long long><<<grid, f32col::NT, 0, s>>>(b);
+        }
         return cudaGetLastError();
     }
 };

@@ -79,6 +79,7 @@ struct BatchParams {
     unsigned* exited;           // CTAs that found the queue empty; the last resets head and itself
     const int* idle;            // grids without interior cells (no work item): finalized by the last CTA
     int nidle;
+    long long max_cells;        // cells of the largest grid (selects 32-bit offsets where they suffice)
 };
 
 template <class T>
