@@ -383,18 +383,21 @@ __device__ __forceinline__ Flux<float> hllc_flux(Side<float> const& L, Side<floa
     float const qrc = left ? rc_L : rc_R;
     float const M = S * den - num;
     float const Rr = rcp_approx(den * M); // |den M| is far from the ends of the float range for any physical state
-    float const ustar = num * (M * Rr);
+    // Supersonic faces take the upwind state's own flux.  ustar := un and
+    // ratio := 1 give it exactly (w = 0, so pstar = p, d_star = d and
+    // h_star = e + p), with two selects instead of four.
+    bool const supersonic = S_L * S_R > 0.0f;
+    float const ustar = supersonic ? qun : num * (M * Rr);
     float const inv = den * (den * Rr);
     float const w = ustar - qun;
     float const pstar = qp + qrc * w;
-    bool const supersonic = S_L * S_R > 0.0f;
-    float const ratio = (S - qun) * inv;
+    float const ratio = supersonic ? 1.0f : (S - qun) * inv;
     float const d_star = ratio * qd;
     float const h_star = ratio * qh + w * (S * d_star); // e_star + pstar
-    float const un_o = supersonic ? qun : ustar;
-    float const ptot_o = supersonic ? qp : pstar;
-    float const d_o = supersonic ? qd : d_star;
-    float const h_o = supersonic ? qh : h_star;
+    float const un_o = ustar;
+    float const ptot_o = pstar;
+    float const d_o = d_star;
+    float const h_o = h_star;
     Flux<float> f;
     f.d = d_o * un_o;
     f.e = h_o * un_o;

@@ -158,20 +158,14 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 // All of this thread's copy groups but the last committed one have landed.
 __device__ __forceinline__ void cp_async_wait_all_but_last() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-// Starts copying the cons of cell (i, j, k) to dst[f * stride] (benign values for cells outside the array).
+// Starts copying the cons of cell (i, j, k) to dst[f * stride].  A cell past
+// the array's last ghost layer (a tile overhanging the grid) takes the state
+// of the nearest ghost cell: physical values, read without a branch, and no
+// face that touches such a cell is used.
 template <class Off>
 __device__ __forceinline__ void prefetch_raw(float* dst, int stride, FluxParams<float> const& p, int i, int j, int k)
 {
-    if (i >= p.g.n0 || j >= p.g.n1) {
-        Raw5 const b = outside();
-        dst[0] = b.d;
-        dst[stride] = b.e;
-        dst[2 * stride] = b.m[0];
-        dst[3 * stride] = b.m[1];
-        dst[4 * stride] = b.m[2];
-        return;
-    }
-    Off const o = cell_offset<Off>(p.g, i, j, k);
+    Off const o = cell_offset<Off>(p.g, min(i, p.g.n0 - 1), min(j, p.g.n1 - 1), k);
 #pragma unroll
     for (int f = 0; f < 5; ++f) {
         cp_async4(dst + f * stride, p.cons_in.f[f] + o);
@@ -200,28 +194,52 @@ __device__ __forceinline__ void halo_cell(int h, int& hx, int& hy)
     }
 }
 
-__device__ __forceinline__ void put(float* q, int idx, Prim7 const& v)
+// One plane slot: a staged cell is two 16-byte words, (d, p, u0, u1) and
+// (u2, c, e + p, -), written and read with two vector accesses (STS.128 and
+// LDS.128) instead of seven scalar ones.  Consecutive lanes touch
+// consecutive words, so the accesses are free of bank conflicts.
+struct SlotPlane {
+    float4 a[PLANE];
+    float4 b[PLANE];
+};
+
+__device__ __forceinline__ void put(SlotPlane& q, int idx, Prim7 const& v)
 {
-    q[0 * PLANE + idx] = v.d;
-    q[1 * PLANE + idx] = v.p;
-    q[2 * PLANE + idx] = v.u[0];
-    q[3 * PLANE + idx] = v.u[1];
-    q[4 * PLANE + idx] = v.u[2];
-    q[5 * PLANE + idx] = v.c;
-    q[6 * PLANE + idx] = v.e;
+    q.a[idx] = make_float4(v.d, v.p, v.u[0], v.u[1]);
+    q.b[idx] = make_float4(v.u[2], v.c, v.e, v.e);
 }
 
-__device__ __forceinline__ Prim7 get(float const* q, int idx)
+__device__ __forceinline__ Prim7 get(SlotPlane const& q, int idx)
 {
+    float4 const a = q.a[idx];
+    float4 const b = q.b[idx];
     Prim7 v;
-    v.d = q[0 * PLANE + idx];
-    v.p = q[1 * PLANE + idx];
-    v.u[0] = q[2 * PLANE + idx];
-    v.u[1] = q[3 * PLANE + idx];
-    v.u[2] = q[4 * PLANE + idx];
-    v.c = q[5 * PLANE + idx];
-    v.e = q[6 * PLANE + idx];
+    v.d = a.x;
+    v.p = a.y;
+    v.u[0] = a.z;
+    v.u[1] = a.w;
+    v.u[2] = b.x;
+    v.c = b.y;
+    v.e = b.z;
     return v;
+}
+
+// Five flux components through shared memory as one 16-byte word and one
+// 4-byte word.
+__device__ __forceinline__ void put_flux(float4* a, float* b, int idx, float const* f)
+{
+    a[idx] = make_float4(f[0], f[1], f[2], f[3]);
+    b[idx] = f[4];
+}
+
+__device__ __forceinline__ void get_flux(float4 const* a, float const* b, int idx, float* f)
+{
+    float4 const v = a[idx];
+    f[0] = v.x;
+    f[1] = v.y;
+    f[2] = v.z;
+    f[3] = v.w;
+    f[4] = b[idx];
 }
 
 // ---- paired FP32 arithmetic: on sm_100 and later, FADD2/FMUL2/FFMA2
@@ -249,9 +267,11 @@ __device__ __forceinline__ float2 comp_update2(float2 u, float2 xl, float2 xr, f
 }
 
 struct ColShared {
-    float slot[2][kFields * PLANE];
-    float yflux[5][NT];
-    float xflux_r[5][TY]; // the tile's right boundary x faces
+    SlotPlane slot[2];
+    float4 yflux_a[NT]; // the y face below each cell
+    float yflux_b[NT];
+    float4 xflux_ra[TY]; // the tile's right boundary x faces
+    float xflux_rb[TY];
     float raw_own[5 * NT];     // own column, two planes ahead
     float raw_halo[5 * NHALO]; // halo ring, one plane ahead
     long long warp_best[NT / 32];
@@ -306,7 +326,7 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
     // of each copy is a constant.
 #pragma unroll 2
     for (int k = kb; k < ke; ++k) {
-        float* const q = sh.slot[(k - kb) & 1];
+        SlotPlane& q = sh.slot[(k - kb) & 1];
         // stage plane k: the own cell (its halo ring was staged a plane ahead)
         put(q, own_idx, q0);
         // own column plane k+2, consumed at the end of this plane
@@ -332,10 +352,7 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
         {
             float t[5];
             to_global(hllc_flux(side_of(get(q, own_idx - HX), 1), side_of(q0, 1)), 1, t);
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                sh.yflux[f][tid] = t[f]; // read back after the barrier (registers are scarce here)
-            }
+            put_flux(sh.yflux_a, sh.yflux_b, tid, t); // read back after the barrier (registers are scarce here)
         }
         to_global(hllc_flux(side_of(get(q, own_idx - 1), 0), side_of(q0, 0)), 0, fxl);
         to_global(hllc_flux(side_of(q0, 2), side_of(q1, 2)), 2, fzh);
@@ -347,23 +364,23 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
             int const c = (ti + 1) * HX + TX;
             float t[5];
             to_global(hllc_flux(side_of(get(q, c), 0), side_of(get(q, c + 1), 0)), 0, t);
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                sh.xflux_r[f][ti] = t[f];
-            }
+            put_flux(sh.xflux_ra, sh.xflux_rb, ti, t);
         }
         if (tj == TY - 1) { // the tile's top boundary faces
             to_global(hllc_flux(side_of(q0, 1), side_of(get(q, own_idx + HX), 1)), 1, fyt);
         }
         __syncthreads(); // y fluxes and right boundary fluxes written
+        get_flux(sh.yflux_a, sh.yflux_b, tid, fyb);
+        if (tj < TY - 1) {
+            get_flux(sh.yflux_a, sh.yflux_b, tid + TX, fyt);
+        }
+        {
+            float xr[5];
+            get_flux(sh.xflux_ra, sh.xflux_rb, tj, xr); // one broadcast read per warp
 #pragma unroll
-        for (int f = 0; f < 5; ++f) {
-            fyb[f] = sh.yflux[f][tid];
-            if (tj < TY - 1) {
-                fyt[f] = sh.yflux[f][tid + TX];
+            for (int f = 0; f < 5; ++f) {
+                fxr[f] = ti == TX - 1 ? xr[f] : fxr[f];
             }
-            float const xr = sh.xflux_r[f][tj]; // one broadcast read per warp
-            fxr[f] = ti == TX - 1 ? xr : fxr[f];
         }
 
         // ---- update of the own cell
