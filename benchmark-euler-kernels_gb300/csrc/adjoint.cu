@@ -48,8 +48,36 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// Division of a cell index (below 2^31) by a grid stride d without a runtime
+// division: q = floor(c m / 2^shift) with l = ceil(log2 d), shift = 31 + l and
+// m = ceil(2^shift / d) < 2^32, exact for every 31-bit dividend (T. Granlund
+// and P. Montgomery, "Division by invariant integers using multiplication",
+// PLDI 1994, theorem 4.2).  A 64-bit division per cell was a library
+// routine of several dozen instructions.
+struct DivMagic {
+    unsigned m;
+    int shift;
+};
+
+DivMagic div_magic(long long d)
+{
+    int l = 0;
+    while ((1ll << l) < d) {
+        ++l;
+    }
+    unsigned long long const two = 1ull << (31 + l);
+    return DivMagic{static_cast<unsigned>((two + static_cast<unsigned long long>(d) - 1) / static_cast<unsigned long long>(d)),
+                    31 + l};
+}
+
+__device__ __forceinline__ int div_by(long long c, DivMagic const& dm)
+{
+    return static_cast<int>((static_cast<unsigned long long>(static_cast<unsigned>(c)) * dm.m) >> dm.shift);
+}
+
 struct AdjParams {
     Geom g;
+    DivMagic by_s1, by_s2; // cell index -> (i, j, k)
     CBundle<double> prim;
     CBundle<double> cbar;
     Bundle<double> out;
@@ -66,12 +94,15 @@ __device__ __forceinline__ bool interior(Geom const& g, int i, int j, int k)
     return i >= 1 && i < g.n0 - 1 && j >= 1 && j < g.n1 - 1 && k >= 1 && k < g.n2 - 1;
 }
 
-__device__ __forceinline__ void decode(Geom const& g, long long c, int& i, int& j, int& k)
+// (i, j, k) of cell index c; grids hold fewer than 2^31 cells (the entry
+// points reject larger ones), so 32-bit arithmetic is exact.
+__device__ __forceinline__ void decode(AdjParams const& p, long long c, int& i, int& j, int& k)
 {
-    k = static_cast<int>(c / g.s2);
-    long long const r = c - static_cast<long long>(k) * g.s2;
-    j = static_cast<int>(r / g.s1);
-    i = static_cast<int>(r - static_cast<long long>(j) * g.s1);
+    int const cc = static_cast<int>(c);
+    k = div_by(cc, p.by_s2);
+    int const r = cc - k * static_cast<int>(p.g.s2);
+    j = div_by(r, p.by_s1);
+    i = r - j * static_cast<int>(p.g.s1);
 }
 
 // Per-cell data of the reverse step for state `prim` at cell c (coordinates
@@ -117,7 +148,7 @@ __global__ void __launch_bounds__(kThreads) adj_prep_kernel(AdjParams p)
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
         int i, j, k;
-        decode(p.g, c, i, j, k);
+        decode(p, c, i, j, k);
         double cb[5];
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
@@ -197,23 +228,30 @@ __global__ void __launch_bounds__(kThreads, 2) adj_face_kernel(AdjParams p)
     unsigned const below = (1u << lane) - 1u;
     long long(*const q)[64] = queue[threadIdx.x >> 5];
     int qn[2] = {0, 0}; // faces queued in this warp, per queue (the same in every lane)
-    int const ext[3] = {p.g.n0, p.g.n1, p.g.n2};
     long long const stride = static_cast<long long>(gridDim.x) * blockDim.x;
     // warp-uniform trip count: every lane of a warp runs every iteration
     for (long long base = blockIdx.x * static_cast<long long>(blockDim.x) + (threadIdx.x & ~31); base < n;
          base += stride) {
         long long const c = base + lane;
         bool const valid = c < n;
-        int idx[3] = {0, 0, 0};
+        int i0 = 0, i1 = 0, i2 = 0;
         if (valid) {
-            decode(p.g, c, idx[0], idx[1], idx[2]);
+            decode(p, c, i0, i1, i2);
         }
 #pragma unroll 1
         for (int a = 0; a < 3; ++a) {
-            int const b = a == 2 ? 0 : a + 1, e = a == 0 ? 2 : a - 1;
+            // the cell's coordinate and the grid's extent along axis a and the
+            // two axes after it, by selects (an array indexed by the loop
+            // counter would live in local memory)
+            int const ia = a == 0 ? i0 : (a == 1 ? i1 : i2);
+            int const ib = a == 0 ? i1 : (a == 1 ? i2 : i0);
+            int const ie = a == 0 ? i2 : (a == 1 ? i0 : i1);
+            int const na = a == 0 ? p.g.n0 : (a == 1 ? p.g.n1 : p.g.n2);
+            int const nb = a == 0 ? p.g.n1 : (a == 1 ? p.g.n2 : p.g.n0);
+            int const ne = a == 0 ? p.g.n2 : (a == 1 ? p.g.n0 : p.g.n1);
             // the face between c and c + e_a is solved by the step when one side is interior
-            bool const active = valid && idx[a] <= ext[a] - 2 && idx[b] >= 1 && idx[b] <= ext[b] - 2 &&
-                                idx[e] >= 1 && idx[e] <= ext[e] - 2;
+            bool const active =
+                    valid && ia <= na - 2 && ib >= 1 && ib <= nb - 2 && ie >= 1 && ie <= ne - 2;
             bool need = false;
             bool quiet = false;
             if (active) {
@@ -274,7 +312,7 @@ __global__ void __launch_bounds__(kThreads) adj_gather_kernel(AdjParams p, CBund
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
         int idx[3];
-        decode(p.g, c, idx[0], idx[1], idx[2]);
+        decode(p, c, idx[0], idx[1], idx[2]);
         double pb[5];
 #pragma unroll
         for (int f = 0; f < 5; ++f) {
@@ -384,6 +422,23 @@ int blocks_for(long long n, int sms, int per_sm)
     return static_cast<int>(b < 1 ? 1 : (b < cap ? b : cap));
 }
 
+// Blocks of `kernel` resident on one SM (queried once per kernel): the face
+// and gather kernels run one resident wave of blocks that stride over the
+// grid, so that no partial last wave idles most of the GPU.
+template <auto Kernel>
+int resident_per_sm()
+{
+    static int const n = [] {
+        int r = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, Kernel, kThreads, 0) != cudaSuccess || r < 1) {
+            (void)cudaGetLastError();
+            r = 1;
+        }
+        return r;
+    }();
+    return n;
+}
+
 size_t pad_field(long long n) { return (static_cast<size_t>(n) * sizeof(double) + 255) & ~static_cast<size_t>(255); }
 
 } // namespace
@@ -414,6 +469,8 @@ AdjParams make_params(CBundle<double> prim, CBundle<double> cbar, Bundle<double>
 {
     AdjParams p;
     p.g = g;
+    p.by_s1 = div_magic(g.s1);
+    p.by_s2 = div_magic(g.s2);
     p.prim = prim;
     p.cbar = cbar;
     p.out = out;
@@ -442,9 +499,9 @@ cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bund
         adj_prep_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
     }
     if (p.unit) {
-        adj_face_kernel<true><<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+        adj_face_kernel<true><<<blocks_for(n, sms, resident_per_sm<adj_face_kernel<true>>()), kThreads, 0, s>>>(p);
     } else {
-        adj_face_kernel<false><<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p);
+        adj_face_kernel<false><<<blocks_for(n, sms, resident_per_sm<adj_face_kernel<false>>()), kThreads, 0, s>>>(p);
     }
     CBundle<double> pv{};
     double ws_prev = 0.0;
@@ -452,7 +509,7 @@ cudaError_t launch_step_adjoint(CBundle<double> prim, CBundle<double> cbar, Bund
         pv = *prev;
         ws_prev = dt_prev / (dx0 * dx1 * dx2) * (p.unit ? p.ds[0] : 1.0);
     }
-    adj_gather_kernel<<<blocks_for(n, sms, 8), kThreads, 0, s>>>(p, pv, ws_prev);
+    adj_gather_kernel<<<blocks_for(n, sms, resident_per_sm<adj_gather_kernel>()), kThreads, 0, s>>>(p, pv, ws_prev);
     return cudaGetLastError();
 }
 

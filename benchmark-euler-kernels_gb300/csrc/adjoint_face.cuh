@@ -39,7 +39,11 @@ EULR_ADJ_FN double adj_rcp(double x)
 EULR_ADJ_FN long long adj_bits(double x)
 {
 #if defined(__CUDA_ARCH__)
-    return __double_as_longlong(x);
+    // an opaque move: the compiler would otherwise turn some bit tests back
+    // into FP64 compares, which take FP64-pipe slots
+    long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return b;
 #else
     long long b;
     std::memcpy(&b, &x, sizeof b);

@@ -60,6 +60,7 @@ struct TileLayout {
     static constexpr int NFY_W = (NFY + 31) / 32 * 32;
     static constexpr int NFACE_W = NFX_W + NFY_W + NFZ;
     static_assert(NFACE_W >= NFACE && NFACE_W - NFACE < 64, "padding of at most one warp per family");
+    static_assert(NFX < 4096 && NFY < 4096 && NFZ < 4096, "face index range of div_small");
     static constexpr int NT = TX * TY;
     // shared memory, in T elements after a 128-byte mbarrier block
     static constexpr int Q_ELEMS = NSLOT * kFields * PLANE_PAD;
@@ -356,7 +357,7 @@ __device__ __forceinline__ bool tile_item(TileCtx<T>& c, FluxParams<T> const& p,
                 bool const is_x = f < L::NFX;
                 bool const is_y = !is_x && f < L::NFX + L::NFY;
                 int const g = is_x ? f : (is_y ? f - L::NFX : f - L::NFX - L::NFY);
-                int const gj = is_x ? g / (TX + 1) : g / TX;
+                int const gj = is_x ? div_small<TX + 1>(g) : div_small<TX>(g);
                 int const gi = g - gj * (is_x ? TX + 1 : TX);
                 int const a = (is_y ? gj : gj + 1) * L::HX + (is_x ? gi : gi + 1);
                 int const dir = is_x ? 0 : (is_y ? 1 : 2);

@@ -98,6 +98,20 @@ __device__ __forceinline__ void to_global(Flux<float> const& f, int dir, float* 
     g[2 + (dir + 2) % 3] = f.t2;
 }
 
+// Pressure (gamma-1) (e - m.u / 2) of an FP32 conservative cell from its
+// velocities u = m / rho: the kinetic energy as m.u instead of |m|^2 / rho
+// saves the product by 1/(2 rho).  Compensated states redo the subtraction
+// in FP64 where it lost more than 8 bits (pressure_f64_rescue).
+template <int COMP>
+__device__ __forceinline__ float col_pressure(Raw5 const& r, float u0, float u1, float u2, float ir, float gm1)
+{
+    float const eint = r.e - 0.5f * (r.m[0] * u0 + r.m[1] * u1 + r.m[2] * u2);
+    if (COMP == kCompNone || eint > kLowPressure * r.e) {
+        return gm1 * eint;
+    }
+    return pressure_f64_rescue(r.d, r.e, r.m[0], r.m[1], r.m[2], ir, gm1, nullptr);
+}
+
 // Primitive state, sound speed and e + p of an FP32 conservative cell.  1/rho
 // is the hardware reciprocal (one MUFU.RCP), not the correctly rounded
 // sequence: the FP32 step's error budget is set by the state's own rounding,
@@ -111,7 +125,7 @@ __device__ __forceinline__ Prim7 prim_of(Raw5 const& r, FluxParams<float> const&
     q.u[0] = r.m[0] * ir;
     q.u[1] = r.m[1] * ir;
     q.u[2] = r.m[2] * ir;
-    q.p = cons_pressure<COMP>(r.d, r.e, r.m[0], r.m[1], r.m[2], ir, p.gm1, nullptr);
+    q.p = col_pressure<COMP>(r, q.u[0], q.u[1], q.u[2], ir, p.gm1);
     q.c = fast_sound_speed(p.gamma * q.p * ir);
     q.e = __fadd_rn(r.e, q.p);
     return q;
@@ -279,7 +293,8 @@ struct ColShared {
 };
 
 // One work item: interior planes [kb, ke) of the 32 x 8 column tile (tx, ty),
-// kb = 1 + kc * kchunk, with update coefficients k0..k2 (all equal when UNIFORM).
+// kb = 1 + kc * kchunk, with update coefficients k0..k2 (UNIFORM: cubic cells, k0..k2
+// all equal and 1/dx_d too).
 // Accumulates this thread's max wavespeed and non-physical flag.
 template <int COMP, bool UNIFORM, class Off>
 __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, float k1, float k2, int tx, int ty,
@@ -431,13 +446,16 @@ __device__ __forceinline__ void col_item(FluxParams<float> const& p, float k0, f
             for (int f = 0; f < 5; ++f) {
                 p.cons_out.f[f][o] = u[f];
             }
-            // next step's CFL wavespeed of the new state (time_step.hpp:28-33)
+            // next step's CFL wavespeed of the new state (time_step.hpp:28-33);
+            // on cubic cells (3 cs + |v0| + |v1| + |v2|) / dx, one product
+            Raw5 const nr{u[0], u[1], {u[2], u[3], u[4]}};
             float const r = rcp_approx(u[0]);
             float const v0 = u[2] * r, v1 = u[3] * r, v2 = u[4] * r;
-            float const pr = cons_pressure<COMP>(u[0], u[1], u[2], u[3], u[4], r, p.gm1, nullptr);
+            float const pr = col_pressure<COMP>(nr, v0, v1, v2, r, p.gm1);
             float const cs = fast_sound_speed((p.gamma * r) * pr);
-            float const invdt = (cs + fabsf(v0)) * p.invdx0 + (cs + fabsf(v1)) * p.invdx1 +
-                                (cs + fabsf(v2)) * p.invdx2;
+            float const invdt = UNIFORM ? (3.0f * cs + fabsf(v0) + fabsf(v1) + fabsf(v2)) * p.invdx0
+                                        : (cs + fabsf(v0)) * p.invdx0 + (cs + fabsf(v1)) * p.invdx1 +
+                                                  (cs + fabsf(v2)) * p.invdx2;
             wmaxf = fmaxf(wmaxf, invdt); // NaN never wins
             bad |= !cell_ok(u[0], pr, invdt);
         }
@@ -517,7 +535,7 @@ __global__ void __launch_bounds__(NT, 3) f32_step_kernel(const __grid_constant__
 
 // The column engine over a batch: CTAs pop (grid, tile x, tile y, chunk)
 // items from the queue, as flux_batch_kernel does; each item's wavespeed goes
-// to its own grid.  Grids with equal face areas take the cubic update.
+// to its own grid.  Grids of cubic cells take the cubic update and wavespeed.
 template <int COMP, class Off>
 __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant__ BatchParams<float> b)
 {
@@ -546,7 +564,7 @@ __global__ void __launch_bounds__(NT, 3) f32_batch_kernel(const __grid_constant_
         __syncthreads();
         float const dtodv = dt_over_dv(gp);
         float const k0 = dtodv * gp.ds0, k1 = dtodv * gp.ds1, k2 = dtodv * gp.ds2;
-        if (gp.ds0 == gp.ds1 && gp.ds1 == gp.ds2) {
+        if (gp.ds0 == gp.ds1 && gp.ds1 == gp.ds2 && gp.invdx0 == gp.invdx1 && gp.invdx1 == gp.invdx2) {
             col_item<COMP, true, Off>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
         } else {
             col_item<COMP, false, Off>(gp, k0, k1, k2, it.y, it.z, it.w, sh, wmaxf, bad);
@@ -592,8 +610,9 @@ cudaError_t launch_f32col(FluxParams<float> p, int sms, cudaStream_t s)
     long long const nwork = static_cast<long long>(p.tiles_x) * p.tiles_y * kchunks;
     p.nwork = static_cast<int>(nwork);
     long long const grid = slots < nwork ? slots : nwork;
-    // equal face areas (cubic cells) give equal update coefficients dt/dv * ds_d
-    bool const uniform = p.ds0 == p.ds1 && p.ds1 == p.ds2;
+    // cubic cells: equal face areas give equal update coefficients dt/dv * ds_d,
+    // and equal 1/dx_d the one-product wavespeed
+    bool const uniform = p.ds0 == p.ds1 && p.ds1 == p.ds2 && p.invdx0 == p.invdx1 && p.invdx1 == p.invdx2;
     if (p.g.ncell() <= kNarrowCells) {
         if (uniform) {
             f32col::f32_step_kernel<COMP, true, unsigned><<<static_cast<int>(grid), f32col::NT, 0, s>>>(p);

@@ -13,6 +13,19 @@ namespace {
 constexpr int kFields = 7; // face inputs of a staged cell: d, p, u0, u1, u2, c, e
 constexpr long long kInfBits = 0x7ff0000000000000LL;
 
+// g / D for 0 <= g < 2^12 and a compile-time 0 < D < 256, as one product and
+// a shift: floor(g (floor(2^20/D) + 1) / 2^20) exceeds g/D by less than
+// g/2^20 < 2^-8, which stays below the gap 1/D to the next integer.  The
+// tile engine's face index takes one of two constant divisors by a select,
+// which the compiler otherwise turned into a runtime integer division.
+template <int D>
+__device__ __forceinline__ int div_small(int g)
+{
+    static_assert(D > 0 && D < 256, "divisor range");
+    constexpr unsigned kM = (1u << 20) / D + 1u;
+    return static_cast<int>((static_cast<unsigned>(g) * kM) >> 20);
+}
+
 __device__ __forceinline__ unsigned smem_u32(const void* p)
 {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
