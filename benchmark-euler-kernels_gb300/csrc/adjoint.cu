@@ -82,7 +82,7 @@ struct AdjParams {
     CBundle<double> cbar;
     Bundle<double> out;
     AdjWork w;
-    double gamma, gm1, inv_gm1;
+    double gamma, gm1, inv_gm1, half_gamma;
     double ds[3];
     bool unit;     // cubic cells: ds is folded into the weights
     double wscale; // dt / dv (times ds when unit)
@@ -128,10 +128,10 @@ __device__ __forceinline__ void prep_cell(AdjParams const& p, CBundle<double> co
     y = __fma_rn(y, e * __fma_rn(0.375, e, 0.5), y); // third-order step, as sqrt_faithful's
     double const cs = gp * y;
     double const inv_d = cs * y;
-    double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+    double const ke = adj_half(u0 * u0 + u1 * u1 + u2 * u2);
     p.w.derived[0][c] = cs;
-    p.w.derived[1][c] = (0.5 * p.gamma) * y;
-    p.w.derived[2][c] = -0.5 * cs * inv_d;
+    p.w.derived[1][c] = p.half_gamma * y;
+    p.w.derived[2][c] = -adj_half(cs * inv_d);
     p.w.derived[3][c] = pr * p.inv_gm1 + d * ke;
     p.w.derived[4][c] = ke;
     p.w.derived[5][c] = inv_d;
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(kThreads) c2p_bar_kernel(CBundle<double> prim,
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
         double const d = prim.f[0][c];
         double const u0 = prim.f[2][c], u1 = prim.f[3][c], u2 = prim.f[4][c];
-        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        double const ke = adj_half(u0 * u0 + u1 * u1 + u2 * u2);
         double const inv_d = rcp_faithful(d);
         double const b0 = pbar.f[0][c], b2 = pbar.f[2][c], b3 = pbar.f[3][c], b4 = pbar.f[4][c];
         double const gp = pbar.f[1][c] * gm1;
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(kThreads) p2c_bar_kernel(CBundle<double> prim,
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
         double const d = prim.f[0][c];
         double const u0 = prim.f[2][c], u1 = prim.f[3][c], u2 = prim.f[4][c];
-        double const ke = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        double const ke = adj_half(u0 * u0 + u1 * u1 + u2 * u2);
         double const c0 = cbar.f[0][c], c1 = cbar.f[1][c], c2 = cbar.f[2][c], c3 = cbar.f[3][c];
         double const c4 = cbar.f[4][c];
         double r[5];
@@ -478,6 +478,7 @@ AdjParams make_params(CBundle<double> prim, CBundle<double> cbar, Bundle<double>
     p.gamma = gamma;
     p.gm1 = gamma - 1.0;
     p.inv_gm1 = 1.0 / (gamma - 1.0);
+    p.half_gamma = 0.5 * gamma;
     p.ds[0] = dx1 * dx2; // uniform_mesh.hpp:33-46
     p.ds[1] = dx2 * dx0;
     p.ds[2] = dx0 * dx1;

@@ -9,6 +9,8 @@
 
 #include <cstring>
 
+#include "halve.cuh"
+
 #if defined(__CUDACC__)
 #define EULR_ADJ_FN __host__ __device__ __forceinline__
 #else
@@ -30,6 +32,19 @@ EULR_ADJ_FN double adj_rcp(double x)
     return __fma_rn(r, e, r);
 #else
     return 1.0 / x;
+#endif
+}
+
+// x * 0.5: on the GPU from the bit pattern on the integer pipe (the same bits
+// as the FP64 multiply, halve.cuh), which saves an FP64 slot.
+EULR_ADJ_FN double adj_half(double x)
+{
+#if defined(__CUDA_ARCH__)
+    unsigned long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return __longlong_as_double(static_cast<long long>(halve_bits(b)));
+#else
+    return x * 0.5;
 #endif
 }
 
@@ -224,7 +239,7 @@ EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, doubl
         inv_den = P * Rr;
         ustar = 0.0;
         double const pstar = q.p - qrc * q.un; // both sides' values agree at num == 0
-        double const hd = 0.5 * gd, he = 0.5 * ge, ht1 = 0.5 * gt1, ht2 = 0.5 * gt2;
+        double const hd = adj_half(gd), he = adj_half(ge), ht1 = adj_half(gt1), ht2 = adj_half(gt2);
         gus = tie_branch_bar(L, aL, (den * SR) * Rr, pstar, hd, he, ht1, ht2) +
               tie_branch_bar(R, aR, (den * SL) * Rr, pstar, hd, he, ht1, ht2);
         gps = gn;
@@ -285,11 +300,11 @@ EULR_ADJ_FN void hllc_bar(FaceSide const& L, FaceSide const& R, double dd, doubl
     bL.un -= gaL;
     bR.un -= gaR;
     // S_L = umin - cmax, S_R = umax + cmax (equal un: half to each side)
-    double const hs = 0.5 * (gSL + gSR);
+    double const hs = adj_half(gSL + gSR);
     bL.un += u_lt ? gSL : (u_gt ? gSR : hs);
     bR.un += u_lt ? gSR : (u_gt ? gSL : hs);
     double const gc = gSR - gSL;
-    double const gcL = c_lt ? 0.0 : (c_gt ? gc : 0.5 * gc);
+    double const gcL = c_lt ? 0.0 : (c_gt ? gc : adj_half(gc));
     double const gcR = gc - gcL;
     bL.p += gcL * L.cp;
     bL.r += gcL * L.cr;

@@ -14,6 +14,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "halve.cuh"
+
 namespace eulr {
 
 template <class T>
@@ -62,6 +64,16 @@ __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, 
 __device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
 __device__ __forceinline__ float sqrt_rn(float a) { return __fsqrt_rn(a); }
 __device__ __forceinline__ double abs_(double a) { return fabs(a); }
+// x * 0.5 with the bits of a DMUL by 0.5, on the integer pipe (halve.cuh);
+// the asm move keeps the compiler from turning the bit arithmetic back into
+// an FP64 multiply.
+__device__ __forceinline__ double half_exact(double x)
+{
+    unsigned long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return __longlong_as_double(static_cast<long long>(halve_bits(b)));
+}
+__device__ __forceinline__ float half_exact(float x) { return __fmul_rn(x, 0.5f); }
 __device__ __forceinline__ float abs_(float a) { return fabsf(a); }
 
 // Correctly rounded x / y given r = RN(1/y): q0 = RN(x r) is within one ulp
@@ -181,7 +193,7 @@ __device__ __forceinline__ void cons_to_prim_exact(T d, T e, T m0, T m1, T m2, T
 {
     T const r = rcp_rn(d);
     T const mm = add_rn(add_rn(mul_rn(m0, m0), mul_rn(m1, m1)), mul_rn(m2, m2));
-    T const ke = mul_rn(div_by_rcp(mm, d, r), T(0.5));
+    T const ke = half_exact(div_by_rcp(mm, d, r));
     p = mul_rn(gm1, sub_rn(e, ke));
     u0 = mul_rn(m0, r);
     u1 = mul_rn(m1, r);
@@ -284,6 +296,20 @@ __device__ __forceinline__ bool product_positive(double a, double b)
 {
     return nonzero_(a) && nonzero_(b) && ((dbits(a) ^ dbits(b)) >= 0);
 }
+
+// a < b with IEEE semantics (false when either is NaN; -0 and +0 equal),
+// decided on the integer pipe: the bit patterns mapped to ordered keys with
+// both zeros at 0.  The same answer as the FP64 compare, which would take an
+// FP64 slot.
+__device__ __forceinline__ bool is_nan_bits(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+__device__ __forceinline__ bool less_ieee(double a, double b)
+{
+    long long const x = dbits(a), y = dbits(b);
+    long long const kx = (x << 1) == 0 ? 0 : (x ^ ((x >> 63) & 0x7fffffffffffffffLL));
+    long long const ky = (y << 1) == 0 ? 0 : (y ^ ((y >> 63) & 0x7fffffffffffffffLL));
+    return !is_nan_bits(x) && !is_nan_bits(y) && kx < ky;
+}
+__device__ __forceinline__ bool less_ieee(float a, float b) { return a < b; }
 
 // Finite and > 0.
 __device__ __forceinline__ bool finite_positive(double x)

@@ -48,16 +48,18 @@ constexpr int kFieldC = 5;
 constexpr int kFieldE = 6;
 
 // Kokkos::min / Kokkos::max on two values (the reference's helpers): the
-// first argument unless the second is strictly smaller / larger.
+// first argument unless the second is strictly smaller / larger.  The
+// comparisons run on the integer pipe with the FP64 compare's answer
+// (less_ieee), so each saves an FP64 slot.
 template <class T>
 __device__ __forceinline__ T kmin(T a, T b)
 {
-    return (b < a) ? b : a;
+    return less_ieee(b, a) ? b : a;
 }
 template <class T>
 __device__ __forceinline__ T kmax(T a, T b)
 {
-    return (a < b) ? b : a;
+    return less_ieee(a, b) ? b : a;
 }
 
 // hllc::operator() (hllc.hpp:50-105) across the face between cell ca of
@@ -80,9 +82,9 @@ __device__ __forceinline__ void solve_face_exact(T const (*A)[kExPC], int ca, T 
     T const rc_R = mul_rn(d_R, sub_rn(S_R, un_R));
     // acoustic star state: q_R.p - q_L.p + rc_L * un_L - rc_R * un_R, left to right
     T const ustar = div_rn(sub_rn(add_rn(sub_rn(p_R, p_L), mul_rn(rc_L, un_L)), mul_rn(rc_R, un_R)), sub_rn(rc_L, rc_R));
-    T const pstar = mul_rn(T(0.5), add_rn(add_rn(add_rn(p_L, p_R), mul_rn(rc_L, sub_rn(ustar, un_L))),
+    T const pstar = half_exact(add_rn(add_rn(add_rn(p_L, p_R), mul_rn(rc_L, sub_rn(ustar, un_L))),
                                           mul_rn(rc_R, sub_rn(ustar, un_R))));
-    bool const left = ustar > T(0);
+    bool const left = less_ieee(T(0), ustar);
     T const (*Q)[kExPC] = left ? A : B;
     int const cq = left ? ca : cb;
     T const S = left ? S_L : S_R;
@@ -90,7 +92,7 @@ __device__ __forceinline__ void solve_face_exact(T const (*A)[kExPC], int ca, T 
     T const p = left ? p_L : p_R;
     T const un = left ? un_L : un_R;
     T const etot = Q[kFieldE][cq];
-    bool const supersonic = mul_rn(S_L, S_R) > T(0);
+    bool const supersonic = less_ieee(T(0), mul_rn(S_L, S_R));
     T const un_o = supersonic ? un : ustar;
     T const ptot_o = supersonic ? p : pstar;
     T const ratio = div_rn(sub_rn(S, un), sub_rn(S, un_o));
@@ -128,7 +130,7 @@ __device__ __forceinline__ void load_plane_exact(T (*P)[kExPC], CBundle<T> const
             P[kFieldC][t] = sqrt_rn(div_rn(mul_rn(gamma, p), d));
             // the reference's "/ 2" as "* 0.5": both are the correctly rounded
             // value of the same real number, so the bits are equal
-            T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
+            T const ke = half_exact(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))));
             P[kFieldE][t] = add_rn(div_by_rcp(p, gm1, rgm1), ke);
         }
     }

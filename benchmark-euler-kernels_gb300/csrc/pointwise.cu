@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) prim_to_cons_kernel(CBundle<T> prim, Bund
         T const u1 = prim.f[3][c];
         T const u2 = prim.f[4][c];
         T const int_e = div_by_rcp(p, gm1, rgm1);
-        T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
+        T const ke = half_exact(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))));
         cons.f[0][c] = d;
         cons.f[1][c] = add_rn(ke, int_e);
         cons.f[2][c] = mul_rn(d, u0);
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256) load_prim_kernel(CBundle<T> prim, Bundle<
             u2 = prim.f[4][c];
             if (cons.f[0] != nullptr) {
                 T const int_e = div_by_rcp(p, gm1, rgm1);
-                T const ke = mul_rn(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))), T(0.5));
+                T const ke = half_exact(mul_rn(d, add_rn(add_rn(mul_rn(u0, u0), mul_rn(u1, u1)), mul_rn(u2, u2))));
                 T const e = add_rn(ke, int_e);
                 cons.f[0][c] = d;
                 cons.f[1][c] = e;
