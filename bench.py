@@ -69,7 +69,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=512, help="interior cells per axis")
-    ap.add_argument("--e2e-steps", type=int, default=16)
+    # the first step's host->device copy and the last step's device->host
+    # copy do not overlap compute; 48 steps amortise them as a stream of
+    # problems does
+    ap.add_argument("--e2e-steps", type=int, default=48)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ops", action="store_true")
