@@ -6,7 +6,8 @@
 // tests/test_gpu_faithful.py.
 //
 // Arguments m * 2^e with m uniform in [1, 2) and e uniform in [-100, 100]
-// (4M of them, a fixed LCG stream), plus the binade edges 1, 2 - ulp, 2^e.
+// (4M of them, a fixed LCG stream), plus the binade edges 1, 2 - ulp, 2^e,
+// and arguments near and beyond FP32's exponent range up to 2^+-400.
 // Prints one line: max ulp distances and the approximations' max relative
 // errors.
 #include "euler_device.cuh"
@@ -66,6 +67,13 @@ int main()
     for (int e = -100; e <= 100; ++e) {
         h.push_back(std::ldexp(1.0, e));
         h.push_back(std::ldexp(std::nextafter(2.0, 1.0), e));
+    }
+    // the seeds' FP32 range ends (2^-125, 2^126) and beyond, where they fall
+    // back to the FP64 approximation
+    for (int e : {-400, -300, -200, -130, -127, -126, -125, -124, 124, 125, 126, 127, 128, 130, 200, 300, 400}) {
+        h.push_back(std::ldexp(1.0, e));
+        h.push_back(std::ldexp(std::nextafter(2.0, 1.0), e));
+        h.push_back(std::ldexp(1.5, e));
     }
     int const n = static_cast<int>(h.size());
     double* dx = nullptr;
