@@ -344,8 +344,8 @@ def run_fp32c_leg(torch, E, args, stream, n0, dx, interior, steps_total, prim_re
                         "achieved": bytes_step / (flux_ms * 1e-3) / 1e9, "peak": hbm_peak,
                         "peak_source": "MEASURED_PEAKS.json (measured)" if hbm_peak else None,
                         "kernel_ms": flux_ms,
-                        "limiter": "instruction issue, not HBM: ncu shows the SM issuing on 71% of cycles at "
-                                   "439 thread-instructions per cell, DRAM at the algorithmic 40 B/cell "
+                        "limiter": "instruction issue, not HBM: ncu shows the SM issuing on 67% of cycles at "
+                                   "409 thread-instructions per cell, DRAM at the algorithmic 40 B/cell "
                                    "(ncu at 256^3)"}}
     if hbm_peak:
         out["roofline"]["frac"] = out["roofline"]["achieved"] / hbm_peak
