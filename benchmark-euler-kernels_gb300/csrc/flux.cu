@@ -178,13 +178,21 @@ __device__ __forceinline__ void load_plane(T* smem, int slot, FluxParams<T> cons
                 cs = fast_sound_speed(p.gamma * pr * r);
             } else {
                 if constexpr (sizeof(T) == 8) {
-                    cs = fast_sound_speed(p.gamma * pr * rcp_faithful(d));
+                    // sqrt(gamma p / rho) from one reciprocal square root, and
+                    // e + p = p gamma/(gamma-1) + (rho/2) |u|^2 with the
+                    // halving on the integer pipe: 4 FP64 instructions and a
+                    // seed fewer per staged cell than 1/rho, a square root
+                    // and e formed before p is added
+                    cs = sqrt_quotient_faithful(p.gamma * pr, d);
+                    e = pr * (p.inv_gm1 + T(1)) + half_exact(d) * (u0 * u0 + u1 * u1 + u2 * u2);
                 } else {
                     cs = sqrt(p.gamma * pr * (T(1) / d));
+                    e = pr * p.inv_gm1 + T(0.5) * d * (u0 * u0 + u1 * u1 + u2 * u2);
                 }
-                e = pr * p.inv_gm1 + T(0.5) * d * (u0 * u0 + u1 * u1 + u2 * u2);
             }
-            e += pr; // the HLLC takes e + p (formed once per staged cell, not per face)
+            if (MODE != kModeGodunov || sizeof(T) == 4) {
+                e += pr; // the HLLC takes e + p (formed once per staged cell, not per face)
+            }
         }
         q[0 * L::PLANE_PAD + c] = d;
         q[1 * L::PLANE_PAD + c] = pr;
