@@ -90,6 +90,38 @@ def test_port_matches_reference_build(oracle_lib):
                 assert np.array_equal(O.cons_to_prim(ca, 1.3, impl=impl_a), O.cons_to_prim(cb, 1.3, impl=impl_b))
 
 
+def test_port_matches_reference_build_on_wide_range_states(oracle_lib):
+    """The wide-range states of the GPU parity test (rho and p log-uniform
+    over [1e-4, 1e4], u ~ N(0, 30^2)): the port equals the reference build bit
+    for bit on every operator and on three steps of the reference loop, so the
+    oracle that test compares against is pinned there too."""
+    O = oracle_lib
+    if not os.path.isdir(os.path.join(O.REFERENCE_DIR, "euler_operators")):
+        pytest.skip("reference checkout not present")
+    O.build(ref=True)
+    rng = np.random.Generator(np.random.PCG64(2026))
+    n0, n1, n2 = 13, 9, 11
+    prim = O.random_prim(n0, n1, n2, seed=1)
+    shape = prim.shape[1:]
+    prim[0] = np.exp(rng.uniform(np.log(1e-4), np.log(1e4), size=shape))
+    prim[1] = np.exp(rng.uniform(np.log(1e-4), np.log(1e4), size=shape))
+    for f in (2, 3, 4):
+        prim[f] = rng.normal(0.0, 30.0, size=shape)
+    prim = np.ascontiguousarray(prim)
+    dx = (1 / 11, 1 / 7, 1 / 9)
+    ca, cb = O.prim_to_cons(prim, 1.4, impl="port"), O.prim_to_cons(prim, 1.4, impl="ref")
+    assert np.array_equal(ca, cb)
+    dt = O.time_step(prim, 1.4, dx, impl="port")
+    assert dt == O.time_step(prim, 1.4, dx, impl="ref")
+    assert np.array_equal(O.godunov(prim, ca, 1.4, dx, 0.4 * dt, impl="port"),
+                          O.godunov(prim, cb, 1.4, dx, 0.4 * dt, impl="ref"))
+    assert np.array_equal(O.cons_to_prim(ca, 1.4, impl="port"), O.cons_to_prim(cb, 1.4, impl="ref"))
+    pa, pb = prim.copy(), prim.copy()
+    ta = O.simulate(pa, ca, 1.4, dx, 0.4, 3, impl="port")
+    tb = O.simulate(pb, cb, 1.4, dx, 0.4, 3, impl="ref")
+    assert ta == tb and np.array_equal(pa, pb) and np.array_equal(ca, cb)
+
+
 def test_implode_64_reference_time(oracle_lib):
     """64^3 implosion, 100 steps at CFL 0.4: the simulated time the reference
     build reaches (0.121580552 to 9 digits)."""
