@@ -90,11 +90,13 @@ def test_port_matches_reference_build(oracle_lib):
                 assert np.array_equal(O.cons_to_prim(ca, 1.3, impl=impl_a), O.cons_to_prim(cb, 1.3, impl=impl_b))
 
 
-def test_port_matches_reference_build_on_wide_range_states(oracle_lib):
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_port_matches_reference_build_on_wide_range_states(oracle_lib, dtype):
     """The wide-range states of the GPU parity test (rho and p log-uniform
     over [1e-4, 1e4], u ~ N(0, 30^2)): the port equals the reference build bit
-    for bit on every operator and on three steps of the reference loop, so the
-    oracle that test compares against is pinned there too."""
+    for bit on every operator and on three steps of the reference loop, in
+    double and in float, so the oracle that test compares against is pinned
+    there too."""
     O = oracle_lib
     if not os.path.isdir(os.path.join(O.REFERENCE_DIR, "euler_operators")):
         pytest.skip("reference checkout not present")
@@ -107,7 +109,7 @@ def test_port_matches_reference_build_on_wide_range_states(oracle_lib):
     prim[1] = np.exp(rng.uniform(np.log(1e-4), np.log(1e4), size=shape))
     for f in (2, 3, 4):
         prim[f] = rng.normal(0.0, 30.0, size=shape)
-    prim = np.ascontiguousarray(prim)
+    prim = np.ascontiguousarray(prim.astype(dtype))
     dx = (1 / 11, 1 / 7, 1 / 9)
     ca, cb = O.prim_to_cons(prim, 1.4, impl="port"), O.prim_to_cons(prim, 1.4, impl="ref")
     assert np.array_equal(ca, cb)
